@@ -1,0 +1,594 @@
+// eik3d_batch.cu -- the batched misfit + gradient plan (adt_batch_*).
+//
+// One evaluation = for every chunk of solves: persistent forward kernel,
+// receiver sampling + misfit + seeds, persistent adjoint kernel, FP64
+// gradient accumulation; then the misfit sum.  The sequence is captured once
+// into a CUDA graph and replayed per evaluation.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "eik3d_batch.h"
+#include "eik3d_batch_kernels.cuh"
+#include "eik3d_common_host.h"
+
+namespace adt {
+
+namespace {
+
+__global__ void k_to_t_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// FP64 near-source initial values: sqrt(dx^2+dy^2+dz^2) * f * h at the 8
+// nodes around each source (scripts/gene_obs.jl:44-51, order ceil/floor).
+template <class T>
+__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  SolveDev& sd = solves[s];
+  const FieldDev<T>& fd = fields[sd.field];
+  const int xs[2] = {sd.xc, sd.xf}, ys[2] = {sd.yc, sd.yf}, zs[2] = {sd.zc, sd.zf};
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int c = 0; c < 2; ++c) {
+        const double dx = sd.sx - xs[a], dy = sd.sy - ys[b], dz = sd.sz - zs[c];
+        const int64_t p = ((int64_t)xs[a] * fd.g.n + ys[b]) * fd.g.l + zs[c];
+        const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                              __dmul_rn(dz, dz)));
+        sd.v0[a * 4 + b * 2 + c] = __dmul_rn(__dmul_rn(r, fd.f64[p]), fd.h);
+      }
+}
+
+__global__ void k_misfit_sum(const double* __restrict__ m, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = __dadd_rn(s, m[i]);
+    *out = s;
+  }
+}
+
+int grid1d(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 8192));
+}
+
+template <class T>
+size_t fwd_warp_smem(int bk) {
+  return (bk == 64 ? (tile_elems(64) + itile_elems(64)) : (tile_elems(32) + itile_elems(32))) *
+         sizeof(T);
+}
+template <class T>
+size_t adj_warp_smem(int bk) {
+  return bk == 64 ? 2 * tile_elems(64) * sizeof(T) + itile_elems(64) * sizeof(uint16_t)
+                  : 2 * tile_elems(32) * sizeof(T) + itile_elems(32) * sizeof(uint16_t);
+}
+
+}  // namespace
+
+// Kernel entry points per (T, BK), resolved at plan creation.
+struct KernelSet {
+  const void* fwd;
+  const void* adj;
+  const void* misfit;
+  const void* grad;
+};
+
+template <class T>
+static KernelSet kernels_for(int bk) {
+  constexpr int MODE = sizeof(T) == 8 ? MODE_EXACT : MODE_STABLE;
+  KernelSet k;
+  if (bk == 64) {
+    k.fwd = (const void*)&k_batch_fwd<T, 64, MODE>;
+    k.adj = (const void*)&k_batch_adj<T, 64>;
+  } else {
+    k.fwd = (const void*)&k_batch_fwd<T, 32, MODE>;
+    k.adj = (const void*)&k_batch_adj<T, 32>;
+  }
+  k.misfit = (const void*)&k_batch_misfit<T>;
+  k.grad = (const void*)&k_batch_grad<T>;
+  return k;
+}
+
+struct BatchPlan {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  adt_batch_opts opts;
+  int bk = 32;
+  bool f64 = false;
+  size_t esz = 4;
+  // fields
+  int nf = 0;
+  std::vector<Geom> geoms;
+  std::vector<double> h;
+  std::vector<int> nsta;
+  std::vector<int64_t> cell_off, sta_off;
+  int64_t ncell_total = 0;
+  // solves
+  int ns = 0;
+  std::vector<int> solve_field;
+  std::vector<int64_t> obs_off;
+  int64_t nobs = 0;
+  std::vector<SolveDev> solves;
+  struct Chunk {
+    int first, count;
+    std::vector<int> order;                           // largest first
+    std::vector<std::vector<int64_t>> field_uoff;     // per field, solve order
+    int64_t dev_order_off;
+    std::vector<int64_t> dev_uoff_off;                // per field offset into d_uoff
+  };
+  std::vector<Chunk> chunks;
+  // device
+  DevBuf d_slow64, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
+  DevBuf d_levels, d_lstart, d_fields, d_solves, d_order, d_uoff;
+  DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
+  int64_t snap_stride = 0;
+  // launch shapes
+  KernelSet ks;
+  int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
+  size_t fwd_smem = 0, adj_smem = 0, mis_smem = 0;
+  // graph and timing
+  cudaGraphExec_t graph = nullptr;
+  std::vector<cudaEvent_t> ev;  // per chunk: fwd0 fwd1 adj0 adj1; then total0 total1
+  bool ran = false;
+  ~BatchPlan() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto e : ev) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+void batch_opts_default(adt_batch_opts* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = ADT_F32;
+  o->tol = 1e-6;
+  o->max_iter = 200;
+  o->adj_max_iter = 200;
+  o->ref_compat = 0;
+  o->near_src_f64 = 2;
+  o->chunk = 0;
+  o->bk = 0;
+  o->warps = 0;
+  o->use_graph = 1;
+}
+
+static int enqueue(BatchPlan& P);
+
+int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* hh,
+                 const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
+                 const int32_t* solve_field, const double* src_xyz, const adt_batch_opts* opts) {
+  *out = nullptr;
+  adt_batch_opts o;
+  batch_opts_default(&o);
+  if (opts) o = *opts;
+  if (n_fields < 1 || n_solves < 1 || !dims || !hh || !nsta || !solve_field || !src_xyz)
+    return set_error(ADT_EINVAL, "batch: need at least one field and one solve");
+  if (o.precision != ADT_F32 && o.precision != ADT_F64)
+    return set_error(ADT_EINVAL, "batch: precision must be ADT_F32 or ADT_F64");
+  if (o.ref_compat && o.precision != ADT_F64)
+    return set_error(ADT_EINVAL, "batch: ref_compat needs ADT_F64");
+  if (o.max_iter < 1 || o.adj_max_iter < 1 || !(o.tol >= 0.0))
+    return set_error(ADT_EINVAL, "batch: bad iteration caps or tolerance");
+  if (o.bk != 0 && o.bk != 32 && o.bk != 64) return set_error(ADT_EINVAL, "batch: bk must be 0, 32 or 64");
+  auto P = std::make_unique<BatchPlan>();
+  P->opts = o;
+  if (o.ref_compat) P->opts.max_iter = std::min(o.max_iter, 20);
+  P->f64 = o.precision == ADT_F64;
+  P->esz = P->f64 ? 8 : 4;
+  int minl = INT_MAX;
+  for (int f = 0; f < n_fields; ++f) {
+    const int m = dims[3 * f], n = dims[3 * f + 1], l = dims[3 * f + 2];
+    if (m < 2 || n < 2 || l < 2 || m > BI * 2047 || n > BJ * 2047)
+      return set_error(ADT_EINVAL, "batch: field %d has bad dimensions %d x %d x %d", f, m, n, l);
+    if (!(hh[f] > 0.0) || !std::isfinite(hh[f]))
+      return set_error(ADT_EINVAL, "batch: field %d has bad spacing", f);
+    if (nsta[f] < 0 || nsta[f] > 1024)
+      return set_error(ADT_EINVAL, "batch: field %d has %d receivers (0..1024 supported)", f, nsta[f]);
+    minl = std::min(minl, l);
+  }
+  P->bk = o.bk ? o.bk : (minl >= 48 ? 64 : 32);
+  P->nf = n_fields;
+  int64_t sofs = 0;
+  for (int f = 0; f < n_fields; ++f) {
+    const Geom g = make_geom(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2], P->bk);
+    if (g.nbz > 1023) return set_error(ADT_EINVAL, "batch: field %d is too deep", f);
+    P->geoms.push_back(g);
+    P->h.push_back(hh[f]);
+    P->nsta.push_back(nsta[f]);
+    P->cell_off.push_back(P->ncell_total);
+    P->sta_off.push_back(sofs);
+    P->ncell_total += g.ncell;
+    for (int q = 0; q < nsta[f]; ++q) {
+      const double* x = sta_xyz + 3 * (sofs + q);
+      if (!(x[0] >= 0 && x[0] <= g.m - 1 && x[1] >= 0 && x[1] <= g.n - 1 && x[2] >= 0 && x[2] <= g.l - 1))
+        return set_error(ADT_EINVAL, "batch: receiver %d of field %d is outside the grid", q, f);
+    }
+    sofs += nsta[f];
+  }
+  P->ns = n_solves;
+  P->obs_off.resize(n_solves + 1, 0);
+  P->solves.resize(n_solves);
+  for (int s = 0; s < n_solves; ++s) {
+    const int f = solve_field[s];
+    if (f < 0 || f >= n_fields) return set_error(ADT_EINVAL, "batch: solve %d names field %d", s, f);
+    const Geom& g = P->geoms[f];
+    const double* x = src_xyz + 3 * s;
+    if (!(x[0] >= 0 && x[0] <= g.m - 1 && x[1] >= 0 && x[1] <= g.n - 1 && x[2] >= 0 && x[2] <= g.l - 1))
+      return set_error(ADT_EINVAL, "batch: source of solve %d is outside its grid", s);
+    SolveDev sd;
+    std::memset(&sd, 0, sizeof sd);
+    sd.field = f;
+    sd.gidx = s;
+    sd.sx = x[0];
+    sd.sy = x[1];
+    sd.sz = x[2];
+    sd.xc = (int)std::ceil(x[0]);
+    sd.xf = (int)std::floor(x[0]);
+    sd.yc = (int)std::ceil(x[1]);
+    sd.yf = (int)std::floor(x[1]);
+    sd.zc = (int)std::ceil(x[2]);
+    sd.zf = (int)std::floor(x[2]);
+    P->solves[s] = sd;
+    P->solve_field.push_back(f);
+    P->obs_off[s + 1] = P->obs_off[s] + nsta[f];
+    P->solves[s].obs_off = P->obs_off[s];
+  }
+  P->nobs = P->obs_off[n_solves];
+  // chunks of consecutive solves
+  const int C = (o.chunk > 0 && o.chunk < n_solves) ? o.chunk : n_solves;
+  int64_t max_cells = 0, max_bricks = 0, max_seeds = 0;
+  int64_t order_total = 0, uoff_total = 0;
+  for (int c0 = 0; c0 < n_solves; c0 += C) {
+    BatchPlan::Chunk ch;
+    ch.first = c0;
+    ch.count = std::min(C, n_solves - c0);
+    ch.order.resize(ch.count);
+    std::iota(ch.order.begin(), ch.order.end(), c0);
+    std::stable_sort(ch.order.begin(), ch.order.end(), [&](int a, int b) {
+      return P->geoms[P->solve_field[a]].ncell > P->geoms[P->solve_field[b]].ncell;
+    });
+    int64_t cells = 0, bricks = 0, seeds = 0;
+    ch.field_uoff.assign(n_fields, {});
+    for (int s = c0; s < c0 + ch.count; ++s) {
+      const Geom& g = P->geoms[P->solve_field[s]];
+      P->solves[s].u_off = cells;
+      P->solves[s].meta_off = bricks;
+      P->solves[s].seed_off = seeds;
+      ch.field_uoff[P->solve_field[s]].push_back(cells);
+      cells += g.ncell;
+      bricks += 2LL * g.nbx * g.nby * g.nbz;
+      seeds += 8LL * P->nsta[P->solve_field[s]];
+    }
+    max_cells = std::max(max_cells, cells);
+    max_bricks = std::max(max_bricks, bricks);
+    max_seeds = std::max(max_seeds, seeds);
+    ch.dev_order_off = order_total;
+    order_total += ch.count;
+    for (int f = 0; f < n_fields; ++f) {
+      ch.dev_uoff_off.push_back(uoff_total);
+      uoff_total += (int64_t)ch.field_uoff[f].size();
+    }
+    P->chunks.push_back(std::move(ch));
+  }
+  // device setup
+  ADT_CUDA(cudaGetDevice(&P->dev));
+  ADT_CUDA(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+  const size_t es = P->esz;
+  auto R = [&](DevBuf& b, size_t bytes) -> int {
+    cudaError_t e = b.reserve(std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return set_error(ADT_ENOMEM, "batch: cudaMalloc of %zu bytes failed", bytes);
+    return ADT_OK;
+  };
+  int rc;
+#define R_(b, n) \
+  if ((rc = R(b, n))) return rc;
+  R_(P->d_slow64, P->ncell_total * 8);
+  R_(P->d_slowT, P->f64 ? 16 : P->ncell_total * 4);
+  R_(P->d_sta, (size_t)sofs * 3 * 8);
+  R_(P->d_tobs, P->nobs * 8);
+  R_(P->d_w, P->nobs * 8);
+  R_(P->d_tpred, P->nobs * 8);
+  R_(P->d_grad, P->ncell_total * 8);
+  R_(P->d_smis, (size_t)n_solves * 8);
+  R_(P->d_mis, 8);
+  R_(P->d_status, (size_t)n_solves * sizeof(adt_solve_status));
+  R_(P->d_solves, (size_t)n_solves * sizeof(SolveDev));
+  R_(P->d_order, (size_t)order_total * 4);
+  R_(P->d_uoff, (size_t)std::max<int64_t>(uoff_total, 1) * 8);
+  R_(P->d_u, (size_t)max_cells * es);
+  R_(P->d_lam, (size_t)max_cells * es);
+  R_(P->d_code, (size_t)max_cells * 2);
+  R_(P->d_meta, (size_t)max_bricks * 4);
+  R_(P->d_sidx, (size_t)std::max<int64_t>(max_seeds, 1) * 8);
+  R_(P->d_sval, (size_t)std::max<int64_t>(max_seeds, 1) * es);
+  R_(P->d_nseed, (size_t)n_solves * 4);
+  R_(P->d_next, (size_t)2 * P->chunks.size() * 4);
+  R_(P->d_counters, 4 * 8);
+  // level lists per field
+  std::vector<uint32_t> lv;
+  std::vector<int> ls;
+  std::vector<int64_t> lv_off, ls_off;
+  for (int f = 0; f < n_fields; ++f) {
+    LevelList L = make_levels(P->geoms[f]);
+    lv_off.push_back((int64_t)lv.size());
+    ls_off.push_back((int64_t)ls.size());
+    lv.insert(lv.end(), L.bricks.begin(), L.bricks.end());
+    ls.insert(ls.end(), L.start.begin(), L.start.end());
+  }
+  R_(P->d_levels, lv.size() * 4);
+  R_(P->d_lstart, ls.size() * 4);
+  ADT_CUDA(cudaMemcpy(P->d_levels.p, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice));
+  ADT_CUDA(cudaMemcpy(P->d_lstart.p, ls.data(), ls.size() * 4, cudaMemcpyHostToDevice));
+  if (sofs) ADT_CUDA(cudaMemcpy(P->d_sta.p, sta_xyz, (size_t)sofs * 3 * 8, cudaMemcpyHostToDevice));
+  // fields
+  if (P->f64) {
+    std::vector<FieldDev<double>> fdv(n_fields);
+    for (int f = 0; f < n_fields; ++f) {
+      fdv[f].g = P->geoms[f];
+      fdv[f].h = P->h[f];
+      fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
+      fdv[f].f = fdv[f].f64;
+      fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
+      fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
+      fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
+      fdv[f].nsta = P->nsta[f];
+    }
+    R_(P->d_fields, n_fields * sizeof(FieldDev<double>));
+    ADT_CUDA(cudaMemcpy(P->d_fields.p, fdv.data(), n_fields * sizeof(FieldDev<double>), cudaMemcpyHostToDevice));
+    P->ks = kernels_for<double>(P->bk);
+  } else {
+    std::vector<FieldDev<float>> fdv(n_fields);
+    for (int f = 0; f < n_fields; ++f) {
+      fdv[f].g = P->geoms[f];
+      fdv[f].h = P->h[f];
+      fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
+      fdv[f].f = P->d_slowT.as<float>() + P->cell_off[f];
+      fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
+      fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
+      fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
+      fdv[f].nsta = P->nsta[f];
+    }
+    R_(P->d_fields, n_fields * sizeof(FieldDev<float>));
+    ADT_CUDA(cudaMemcpy(P->d_fields.p, fdv.data(), n_fields * sizeof(FieldDev<float>), cudaMemcpyHostToDevice));
+    P->ks = kernels_for<float>(P->bk);
+  }
+  ADT_CUDA(cudaMemcpy(P->d_solves.p, P->solves.data(), n_solves * sizeof(SolveDev), cudaMemcpyHostToDevice));
+  {
+    std::vector<int> ord;
+    std::vector<int64_t> uo;
+    for (auto& ch : P->chunks) {
+      ord.insert(ord.end(), ch.order.begin(), ch.order.end());
+      for (int f = 0; f < n_fields; ++f) uo.insert(uo.end(), ch.field_uoff[f].begin(), ch.field_uoff[f].end());
+    }
+    ADT_CUDA(cudaMemcpy(P->d_order.p, ord.data(), ord.size() * 4, cudaMemcpyHostToDevice));
+    if (!uo.empty()) ADT_CUDA(cudaMemcpy(P->d_uoff.p, uo.data(), uo.size() * 8, cudaMemcpyHostToDevice));
+  }
+  // launch shapes: as many warps (bricks in flight) as shared memory allows
+  int sm_count = 0, smem_optin = 0;
+  ADT_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, P->dev));
+  ADT_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->dev));
+  const size_t budget = (size_t)smem_optin - 1024;
+  const size_t fw = P->f64 ? fwd_warp_smem<double>(P->bk) : fwd_warp_smem<float>(P->bk);
+  const size_t aw = P->f64 ? adj_warp_smem<double>(P->bk) : adj_warp_smem<float>(P->bk);
+  P->fwd_warps = (int)std::min<size_t>(16, budget / fw);
+  P->adj_warps = (int)std::min<size_t>(16, budget / aw);
+  if (o.warps > 0) {
+    P->fwd_warps = std::min(P->fwd_warps, (int)o.warps);
+    P->adj_warps = std::min(P->adj_warps, (int)o.warps);
+  }
+  if (P->fwd_warps < 1 || P->adj_warps < 1)
+    return set_error(ADT_EINVAL, "batch: brick tile does not fit in shared memory");
+  P->fwd_smem = P->fwd_warps * fw;
+  P->adj_smem = P->adj_warps * aw;
+  int maxsta = 0;
+  for (int f = 0; f < n_fields; ++f) maxsta = std::max(maxsta, P->nsta[f]);
+  int pw = 1;
+  while (pw < 8 * maxsta) pw <<= 1;
+  P->mis_smem = (size_t)pw * 16 + (size_t)maxsta * 8 + 16;
+  ADT_CUDA(cudaFuncSetAttribute(P->ks.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->fwd_smem));
+  ADT_CUDA(cudaFuncSetAttribute(P->ks.adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->adj_smem));
+  ADT_CUDA(cudaFuncSetAttribute(P->ks.misfit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->mis_smem));
+  int occ_f = 0, occ_a = 0;
+  ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, P->ks.fwd, P->fwd_warps * 32, P->fwd_smem));
+  ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, P->ks.adj, P->adj_warps * 32, P->adj_smem));
+  P->fwd_ctas = std::max(1, occ_f) * sm_count;
+  P->adj_ctas = std::max(1, occ_a) * sm_count;
+  if (P->opts.ref_compat) {
+    int64_t maxc = 0;
+    for (auto& g : P->geoms) maxc = std::max(maxc, g.ncell);
+    P->snap_stride = maxc;
+    R_(P->d_snap, (size_t)maxc * es * P->fwd_ctas);
+  }
+#undef R_
+  P->ev.resize(4 * P->chunks.size() + 2);
+  for (auto& e : P->ev) ADT_CUDA(cudaEventCreate(&e));
+  *out = P.release();
+  return ADT_OK;
+}
+
+void batch_destroy(BatchPlan* P) { delete P; }
+
+template <class T>
+static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int which_counter) {
+  BatchArgs<T> A;
+  A.fields = P.d_fields.as<FieldDev<T>>();
+  A.solves = P.d_solves.as<SolveDev>();
+  A.order = P.d_order.as<int>() + ch.dev_order_off;
+  A.n_solves = ch.count;
+  A.u = P.d_u.as<T>();
+  A.lam = P.d_lam.as<T>();
+  A.code = P.d_code.as<uint16_t>();
+  A.meta = P.d_meta.as<int>();
+  A.seed_idx = P.d_sidx.as<int64_t>();
+  A.seed_val = P.d_sval.as<T>();
+  A.n_seed = P.d_nseed.as<int>();
+  A.snap = P.opts.ref_compat ? P.d_snap.as<T>() : nullptr;
+  A.snap_stride = P.snap_stride;
+  A.next = P.d_next.as<int>() + which_counter;
+  A.status = P.d_status.as<adt_solve_status>();
+  A.counters = P.d_counters.as<unsigned long long>();
+  A.tol = P.opts.tol;
+  A.max_iter = P.opts.max_iter;
+  A.adj_max_iter = P.opts.adj_max_iter;
+  A.ref_compat = P.opts.ref_compat;
+  A.near_r = P.opts.near_src_f64;
+  return A;
+}
+
+template <class T>
+static int enqueue_t(BatchPlan& P) {
+  cudaStream_t st = P.stream;
+  if (!P.f64)
+    k_to_t_f32<<<grid1d(P.ncell_total), 256, 0, st>>>(P.d_slow64.as<double>(), P.d_slowT.as<float>(),
+                                                      P.ncell_total);
+  k_src_init<T><<<(P.ns + 127) / 128, 128, 0, st>>>(P.d_solves.as<SolveDev>(), P.ns,
+                                                     P.d_fields.as<FieldDev<T>>());
+  ADT_CUDA(cudaMemsetAsync(P.d_grad.p, 0, P.ncell_total * 8, st));
+  ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
+  ADT_CUDA(cudaMemsetAsync(P.d_next.p, 0, 2 * P.chunks.size() * 4, st));
+  ADT_CUDA(cudaEventRecord(P.ev[4 * P.chunks.size()], st));
+  for (size_t c = 0; c < P.chunks.size(); ++c) {
+    const auto& ch = P.chunks[c];
+    BatchArgs<T> Af = make_args<T>(P, ch, (int)(2 * c));
+    BatchArgs<T> Aa = make_args<T>(P, ch, (int)(2 * c + 1));
+    const int gf = std::min(P.fwd_ctas, ch.count);
+    const int ga = std::min(P.adj_ctas, ch.count);
+    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 0], st));
+    {
+      void* args[] = {&Af};
+      ADT_CUDA(cudaLaunchKernel(P.ks.fwd, dim3(gf), dim3(P.fwd_warps * 32), args, P.fwd_smem, st));
+    }
+    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 1], st));
+    {
+      const double* tobs = P.d_tobs.as<double>();
+      const double* w = P.d_w.as<double>();
+      double* tp = P.d_tpred.as<double>();
+      double* sm = P.d_smis.as<double>();
+      void* args[] = {&Af, &tobs, &w, &tp, &sm};
+      ADT_CUDA(cudaLaunchKernel(P.ks.misfit, dim3(ch.count), dim3(256), args, P.mis_smem, st));
+    }
+    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 2], st));
+    {
+      void* args[] = {&Aa};
+      ADT_CUDA(cudaLaunchKernel(P.ks.adj, dim3(ga), dim3(P.adj_warps * 32), args, P.adj_smem, st));
+    }
+    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 3], st));
+    for (int f = 0; f < P.nf; ++f) {
+      const int cnt = (int)ch.field_uoff[f].size();
+      if (!cnt) continue;
+      const T* lam = P.d_lam.as<T>();
+      const int64_t* uo = P.d_uoff.as<int64_t>() + ch.dev_uoff_off[f];
+      const double* f64 = P.d_slow64.as<double>() + P.cell_off[f];
+      double hh = P.h[f];
+      int64_t nc = P.geoms[f].ncell;
+      double* gr = P.d_grad.as<double>() + P.cell_off[f];
+      int cc = cnt;
+      void* args[] = {&lam, &uo, &cc, &f64, &hh, &nc, &gr};
+      ADT_CUDA(cudaLaunchKernel(P.ks.grad, dim3(grid1d(nc)), dim3(256), args, 0, st));
+    }
+  }
+  k_misfit_sum<<<1, 32, 0, st>>>(P.d_smis.as<double>(), P.ns, P.d_mis.as<double>());
+  ADT_CUDA(cudaEventRecord(P.ev[4 * P.chunks.size() + 1], st));
+  ADT_CUDA(cudaGetLastError());
+  return ADT_OK;
+}
+
+static int enqueue(BatchPlan& P) { return P.f64 ? enqueue_t<double>(P) : enqueue_t<float>(P); }
+
+int batch_upload(BatchPlan* P, const double* slowness, const double* t_obs, const double* weight) {
+  if (slowness) {
+    for (int64_t i = 0; i < P->ncell_total; ++i)
+      if (!(slowness[i] > 0.0) || !std::isfinite(slowness[i]))
+        return set_error(ADT_EINVAL, "batch: slowness must be finite and > 0 (cell %lld)", (long long)i);
+    ADT_CUDA(cudaMemcpyAsync(P->d_slow64.p, slowness, P->ncell_total * 8, cudaMemcpyHostToDevice, P->stream));
+  }
+  if (t_obs) ADT_CUDA(cudaMemcpyAsync(P->d_tobs.p, t_obs, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
+  if (weight) ADT_CUDA(cudaMemcpyAsync(P->d_w.p, weight, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
+  return ADT_OK;
+}
+
+int batch_run_resident(BatchPlan* P) {
+  if (!P->opts.use_graph) {
+    int rc = enqueue(*P);
+    if (rc) return rc;
+    P->ran = true;
+    return ADT_OK;
+  }
+  if (!P->graph) {
+    cudaGraph_t g = nullptr;
+    ADT_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue(*P);
+    cudaError_t e = cudaStreamEndCapture(P->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&P->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGraphInstantiate");
+  }
+  ADT_CUDA(cudaGraphLaunch(P->graph, P->stream));
+  P->ran = true;
+  return ADT_OK;
+}
+
+int batch_download(BatchPlan* P, double* misfit, double* t_pred, double* grad,
+                   adt_solve_status* status) {
+  if (misfit) ADT_CUDA(cudaMemcpyAsync(misfit, P->d_mis.p, 8, cudaMemcpyDeviceToHost, P->stream));
+  if (t_pred) ADT_CUDA(cudaMemcpyAsync(t_pred, P->d_tpred.p, P->nobs * 8, cudaMemcpyDeviceToHost, P->stream));
+  if (grad) ADT_CUDA(cudaMemcpyAsync(grad, P->d_grad.p, P->ncell_total * 8, cudaMemcpyDeviceToHost, P->stream));
+  if (status)
+    ADT_CUDA(cudaMemcpyAsync(status, P->d_status.p, P->ns * sizeof(adt_solve_status), cudaMemcpyDeviceToHost,
+                             P->stream));
+  ADT_CUDA(cudaStreamSynchronize(P->stream));
+  return ADT_OK;
+}
+
+int batch_stats(BatchPlan* P, adt_batch_stats* s) {
+  std::memset(s, 0, sizeof(*s));
+  s->bk = P->bk;
+  s->warps = P->fwd_warps;
+  s->ctas = P->fwd_ctas;
+  s->fwd_ms = s->adj_ms = s->total_ms = -1.f;
+  if (!P->ran) return ADT_OK;
+  ADT_CUDA(cudaStreamSynchronize(P->stream));
+  unsigned long long c[4];
+  ADT_CUDA(cudaMemcpy(c, P->d_counters.p, sizeof c, cudaMemcpyDeviceToHost));
+  s->fwd_cell_updates = (int64_t)c[0];
+  s->fwd_bricks = (int64_t)c[1];
+  s->adj_cell_updates = (int64_t)c[2];
+  s->adj_bricks = (int64_t)c[3];
+  float fw = 0.f, aw = 0.f, tot = 0.f, t;
+  for (size_t ch = 0; ch < P->chunks.size(); ++ch) {
+    ADT_CUDA(cudaEventElapsedTime(&t, P->ev[4 * ch], P->ev[4 * ch + 1]));
+    fw += t;
+    ADT_CUDA(cudaEventElapsedTime(&t, P->ev[4 * ch + 2], P->ev[4 * ch + 3]));
+    aw += t;
+  }
+  ADT_CUDA(cudaEventElapsedTime(&tot, P->ev[4 * P->chunks.size()], P->ev[4 * P->chunks.size() + 1]));
+  s->fwd_ms = fw;
+  s->adj_ms = aw;
+  s->total_ms = tot;
+  return ADT_OK;
+}
+
+void* batch_stream(BatchPlan* P) { return (void*)P->stream; }
+
+void* batch_device_buffer(BatchPlan* P, int which) {
+  switch (which) {
+    case 0: return P->d_slow64.p;
+    case 1: return P->d_grad.p;
+    case 2: return P->d_tpred.p;
+    case 3: return P->d_mis.p;
+    default: return nullptr;
+  }
+}
+
+}  // namespace adt

@@ -1,0 +1,22 @@
+// eik3d_batch.h -- batched misfit + gradient plan (host side).
+#pragma once
+#include "../../include/adtomo_gpu.h"
+
+namespace adt {
+
+struct BatchPlan;
+
+void batch_opts_default(adt_batch_opts* o);
+int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* h,
+                 const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
+                 const int32_t* solve_field, const double* src_xyz, const adt_batch_opts* opts);
+void batch_destroy(BatchPlan* p);
+int batch_upload(BatchPlan* p, const double* slowness, const double* t_obs, const double* weight);
+int batch_run_resident(BatchPlan* p);
+int batch_download(BatchPlan* p, double* misfit, double* t_pred, double* grad,
+                   adt_solve_status* status);
+int batch_stats(BatchPlan* p, adt_batch_stats* s);
+void* batch_stream(BatchPlan* p);
+void* batch_device_buffer(BatchPlan* p, int which);
+
+}  // namespace adt

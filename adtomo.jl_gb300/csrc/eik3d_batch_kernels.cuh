@@ -1,0 +1,564 @@
+// eik3d_batch_kernels.cuh -- kernels of the batched misfit + gradient plan.
+//
+// A persistent grid of CTAs; each CTA takes one solve at a time from a work
+// counter (solves pre-sorted largest grid first) and runs that solve's whole
+// forward (or adjoint) alone, so a CTA needs no other CTA: the only
+// synchronisation is __syncthreads between brick levels.  Inside a solve the
+// CTA's warps sweep the bricks of one level concurrently (eik3d_brick.cuh).
+//
+// Brick skipping (exact): a brick is swept in an ordering only if it, or one
+// of its six face neighbours, changed since the brick was last swept.  A
+// sweep of a brick whose cells and halo are unchanged since its last sweep
+// reproduces the same values (the update reads only those), so skipping it
+// leaves every result bit-identical to sweeping everything.
+#pragma once
+#include "eik3d_brick.cuh"
+
+namespace adt {
+
+template <class T>
+struct FieldDev {
+  Geom g;
+  double h;
+  const T* f;               // slowness, compute precision
+  const double* f64;        // slowness, FP64 (near-source initial values, gradient)
+  const uint32_t* bricks;   // level-ordered bricks
+  const int* lstart;        // nlev + 1
+  const double* sta;        // receivers, 3 per station
+  int nsta;
+};
+
+struct SolveDev {
+  int field;
+  int gidx;                 // index in the caller's solve list
+  int xc, xf, yc, yf, zc, zf;  // ceil / floor of the source coordinates
+  double sx, sy, sz;
+  double v0[8];             // initial values at the 8 nodes, FP64 (src init kernel)
+  int64_t u_off;            // cell offset in the chunk buffers
+  int64_t meta_off;         // brick offset in the chunk meta buffer
+  int64_t obs_off;          // pick offset
+  int64_t seed_off;         // seed slot offset (8 per station) in the chunk seed buffer
+};
+
+template <class T>
+struct BatchArgs {
+  const FieldDev<T>* fields;
+  SolveDev* solves;         // all solves (global index)
+  const int* order;         // chunk solves to run, largest first (global indices)
+  int n_solves;             // in this chunk
+  T* u;                     // chunk travel times
+  T* lam;                   // chunk adjoint variables
+  uint16_t* code;           // chunk adjoint codes
+  int* meta;                // chunk brick meta: mod[nb] then proc[nb] per solve
+  int64_t* seed_idx;        // chunk seeds (sorted, merged)
+  T* seed_val;
+  int* n_seed;              // per chunk-local solve... indexed by global solve
+  T* snap;                  // per-CTA snapshot (reference stopping rule), or null
+  int64_t snap_stride;
+  int* next;                // work counter
+  adt_solve_status* status; // per global solve
+  unsigned long long* counters;  // [0] fwd cell updates [1] fwd bricks [2] adj updates [3] adj bricks
+  double tol;
+  int max_iter;
+  int adj_max_iter;
+  int ref_compat;
+  int near_r;
+};
+
+// Initial value of the implicit u0 (scripts/gene_obs.jl:44-51): 1000, or the
+// FP64 distance value at the 8 nodes around the source.
+__device__ __forceinline__ double u0_at(const SolveDev& s, int i, int j, int k) {
+  const bool xi = (i == s.xc) || (i == s.xf);
+  const bool yj = (j == s.yc) || (j == s.yf);
+  const bool zk = (k == s.zc) || (k == s.zf);
+  if (!(xi && yj && zk)) return 1000.0;
+  const int a = (i == s.xc) ? 0 : 1, b = (j == s.yc) ? 0 : 1, c = (k == s.zc) ? 0 : 1;
+  return s.v0[a * 4 + b * 2 + c];
+}
+
+template <class T>
+__device__ __forceinline__ unsigned long long to_ordered(T v);
+template <>
+__device__ __forceinline__ unsigned long long to_ordered<float>(float v) {
+  return (unsigned long long)__float_as_uint(v);
+}
+template <>
+__device__ __forceinline__ unsigned long long to_ordered<double>(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+template <class T>
+__device__ __forceinline__ T from_ordered(unsigned long long b);
+template <>
+__device__ __forceinline__ float from_ordered<float>(unsigned long long b) {
+  return __uint_as_float((unsigned)b);
+}
+template <>
+__device__ __forceinline__ double from_ordered<double>(unsigned long long b) {
+  return __longlong_as_double((long long)b);
+}
+
+// Does brick b need a sweep at time t?  (lanes 0..6 read the meta words)
+__device__ __forceinline__ bool brick_needed(const int* mod, const int* proc, const Geom& g,
+                                             const BrickPos& p, int lane) {
+  const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
+  const int pr = proc[b];
+  int nb = -1;
+  switch (lane) {
+    case 0: nb = b; break;
+    case 1: nb = (p.bx > 0) ? b - g.nby * g.nbz : -1; break;
+    case 2: nb = (p.bx < g.nbx - 1) ? b + g.nby * g.nbz : -1; break;
+    case 3: nb = (p.by > 0) ? b - g.nbz : -1; break;
+    case 4: nb = (p.by < g.nby - 1) ? b + g.nbz : -1; break;
+    case 5: nb = (p.bz > 0) ? b - 1 : -1; break;
+    case 6: nb = (p.bz < g.nbz - 1) ? b + 1 : -1; break;
+    default: break;
+  }
+  bool v = false;
+  if (nb >= 0) {
+    const int md = mod[nb];
+    v = (lane == 0) ? (md >= pr) : (md > pr);
+  }
+  return __any_sync(0xffffffffu, v);
+}
+
+// ------------------------------------------------------------------ forward
+template <class T, int BK, int MODE>
+__global__ void k_batch_fwd(BatchArgs<T> A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_q;
+  __shared__ unsigned long long s_err;
+  const int NW = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* S = reinterpret_cast<T*>(smem) + warp * (tile_elems(BK) + itile_elems(BK));
+  T* F = S + tile_elems(BK);
+  unsigned long long cnt_upd = 0, cnt_brk = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_q = atomicAdd(A.next, 1);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();
+    if (q >= A.n_solves) break;
+    const int gs = A.order[q];
+    const SolveDev sd = A.solves[gs];
+    const FieldDev<T> fd = A.fields[sd.field];
+    const Geom g = fd.g;
+    const T h = (T)fd.h;
+    T* u = A.u + sd.u_off;
+    const int nb = g.nbx * g.nby * g.nbz;
+    int* mod = A.meta + sd.meta_off;
+    int* proc = mod + nb;
+    // u = u0 (column-wise: lanes along k)
+    for (int64_t col = warp; col < (int64_t)g.m * g.n; col += NW) {
+      const int i = (int)(col / g.n), j = (int)(col % g.n);
+      T* uc = u + col * g.l;
+      for (int k = lane; k < g.l; k += 32) uc[k] = (T)u0_at(sd, i, j, k);
+    }
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      mod[b] = -1;
+      proc[b] = -1;
+    }
+    NearBox box;
+    box.i0 = max(0, sd.xf - A.near_r);
+    box.i1 = min(g.m - 1, sd.xc + A.near_r);
+    box.j0 = max(0, sd.yf - A.near_r);
+    box.j1 = min(g.n - 1, sd.yc + A.near_r);
+    box.k0 = max(0, sd.zf - A.near_r);
+    box.k1 = min(g.l - 1, sd.zc + A.near_r);
+    const bool use_near = (A.near_r >= 0) && (MODE == MODE_STABLE);
+    T* snap = A.snap ? A.snap + blockIdx.x * A.snap_stride : nullptr;
+    __syncthreads();
+    int it;
+    bool conv = false;
+    T err = T(0);
+    for (it = 0; it < A.max_iter; ++it) {
+      if (threadIdx.x == 0) s_err = 0ull;
+      if (snap)
+        for (int64_t c = threadIdx.x; c < g.ncell; c += blockDim.x) snap[c] = u[c];
+      __syncthreads();
+      T md = T(0);
+      for (int o = 0; o < 8; ++o) {
+        int si, sj, sk;
+        ordering3(o, si, sj, sk);
+        const int CS = tile_col_stride(BK, sj == sk);
+        for (int d = 0; d < g.nlev; ++d) {
+          const int t = (it * 8 + o) * g.nlev + d;
+          const int q1 = fd.lstart[d + 1];
+          for (int qq = fd.lstart[d] + warp; qq < q1; qq += NW) {
+            const BrickPos p = brick_pos<BK>(g, fd.bricks[qq], si, sj, sk);
+            if (!brick_needed(mod, proc, g, p, lane)) continue;
+            load_halo_tile<T, BK>(S, u, g, p, CS, lane);
+            load_interior<T, BK>(F, fd.f, g, p, CS, lane);
+            cp_async_wait_all();
+            __syncwarp();
+            const bool ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
+                                                         use_near && box.hits(p), lane, md);
+            if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
+            __syncwarp();
+            if (lane == 0) {
+              const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
+              proc[b] = t;
+              if (ch) mod[b] = t;
+              cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
+              cnt_brk += 1;
+            }
+          }
+          __syncthreads();
+        }
+      }
+      if (snap) {
+        T mx = T(0);
+        for (int64_t c = threadIdx.x; c < g.ncell; c += blockDim.x) {
+          const T dd = u[c] > snap[c] ? u[c] - snap[c] : snap[c] - u[c];
+          mx = rmax(dd, mx);
+        }
+        md = mx;
+      }
+      md = warp_max(md);
+      if (lane == 0) atomicMax(&s_err, to_ordered<T>(md));
+      __syncthreads();
+      err = from_ordered<T>(s_err);
+      __syncthreads();
+      if ((double)err < A.tol) {
+        conv = true;
+        break;
+      }
+    }
+    if (threadIdx.x == 0) {
+      adt_solve_status& st = A.status[sd.gidx];
+      st.iters = conv ? it + 1 : it;
+      st.converged = conv ? 1 : 0;
+      st.final_err = (double)err;
+    }
+  }
+  if (lane == 0 && cnt_brk) {
+    atomicAdd(&A.counters[0], cnt_upd);
+    atomicAdd(&A.counters[1], cnt_brk);
+  }
+}
+
+// ---------------------------------------------------------- misfit, seeds
+// One CTA per solve of the chunk.  Samples u at the receivers with the
+// branch structure of scripts/inversion.jl:64-95, forms the weighted misfit
+// (missing picks t_obs == -1 skipped, :81) and the sensitivities dL/du at
+// the (up to 8) nodes of each receiver; equal nodes are merged in
+// (receiver, node) order so the seed values are independent of scheduling.
+template <class T>
+__global__ void k_batch_misfit(BatchArgs<T> A, const double* __restrict__ t_obs,
+                               const double* __restrict__ weight, double* __restrict__ t_pred,
+                               double* __restrict__ solve_misfit) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int gs = A.order[blockIdx.x];
+  const SolveDev sd = A.solves[gs];
+  const FieldDev<T> fd = A.fields[sd.field];
+  const Geom g = fd.g;
+  const T* u = A.u + sd.u_off;
+  const int S = fd.nsta;
+  int E = 8 * S;
+  int P = 1;
+  while (P < E) P <<= 1;
+  long long* key = reinterpret_cast<long long*>(smem);
+  double* val = reinterpret_cast<double*>(key + P);
+  double* mis = val + P;
+  for (int q = threadIdx.x; q < S; q += blockDim.x) {
+    const double x = fd.sta[3 * q], y = fd.sta[3 * q + 1], z = fd.sta[3 * q + 2];
+    const int x1 = (int)floor(x), x2 = (int)ceil(x);
+    const int y1 = (int)floor(y), y2 = (int)ceil(y);
+    const int z1 = (int)floor(z), z2 = (int)ceil(z);
+    auto U = [&](int i, int j, int k) -> double {
+      return (double)u[((int64_t)i * g.n + j) * g.l + k];
+    };
+    double t11, t12, t21, t22, wx1, wx2, wy1, wy2, wz1, wz2;
+    if (x1 == x2) {
+      t11 = U(x1, y1, z1); t12 = U(x1, y1, z2); t21 = U(x1, y2, z1); t22 = U(x1, y2, z2);
+      wx1 = 1.0; wx2 = 0.0;
+    } else {
+      wx1 = x2 - x; wx2 = x - x1;
+      t11 = __dadd_rn(__dmul_rn(wx1, U(x1, y1, z1)), __dmul_rn(wx2, U(x2, y1, z1)));
+      t12 = __dadd_rn(__dmul_rn(wx1, U(x1, y1, z2)), __dmul_rn(wx2, U(x2, y1, z2)));
+      t21 = __dadd_rn(__dmul_rn(wx1, U(x1, y2, z1)), __dmul_rn(wx2, U(x2, y2, z1)));
+      t22 = __dadd_rn(__dmul_rn(wx1, U(x1, y2, z2)), __dmul_rn(wx2, U(x2, y2, z2)));
+    }
+    double t1, t2;
+    if (y1 == y2) {
+      t1 = t11; t2 = t12; wy1 = 1.0; wy2 = 0.0;
+    } else {
+      wy1 = y2 - y; wy2 = y - y1;
+      t1 = __dadd_rn(__dmul_rn(wy1, t11), __dmul_rn(wy2, t21));
+      t2 = __dadd_rn(__dmul_rn(wy1, t12), __dmul_rn(wy2, t22));
+    }
+    double t;
+    if (z1 == z2) {
+      t = t1; wz1 = 1.0; wz2 = 0.0;
+    } else {
+      wz1 = z2 - z; wz2 = z - z1;
+      t = __dadd_rn(__dmul_rn(wz1, t1), __dmul_rn(wz2, t2));
+    }
+    const int64_t o = sd.obs_off + q;
+    t_pred[o] = t;
+    const double to = t_obs[o], w = weight[o];
+    double dt = 0.0, mq = 0.0;
+    if (to != -1.0) {
+      const double r = __dsub_rn(to, t);
+      mq = __dmul_rn(__dmul_rn(w, r), r);
+      dt = __dmul_rn(__dmul_rn(-2.0, w), r);
+    }
+    mis[q] = mq;
+    const int xi[2] = {x1, x2}, yi[2] = {y1, y2}, zi[2] = {z1, z2};
+    const double xw[2] = {wx1, wx2}, yw[2] = {wy1, wy2}, zw[2] = {wz1, wz2};
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const int e = q * 8 + a * 4 + b * 2 + c;
+          const double wt = __dmul_rn(__dmul_rn(xw[a], yw[b]), zw[c]);
+          const double v = __dmul_rn(dt, wt);
+          const long long cell = ((long long)xi[a] * g.n + yi[b]) * g.l + zi[c];
+          // zero contributions leave the accumulated value unchanged: drop them
+          key[e] = (v == 0.0) ? LLONG_MAX : (cell << 16) | e;
+          val[e] = v;
+        }
+  }
+  for (int e = E + threadIdx.x; e < P; e += blockDim.x) key[e] = LLONG_MAX;
+  __syncthreads();
+  // bitonic sort of (key, val) ascending; keys are unique except LLONG_MAX
+  for (int k = 2; k <= P; k <<= 1)
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int ixj = i ^ jj;
+        if (ixj > i) {
+          const bool up = ((i & k) == 0);
+          const long long ki = key[i], kj = key[ixj];
+          if ((ki > kj) == up) {
+            key[i] = kj;
+            key[ixj] = ki;
+            const double tv = val[i];
+            val[i] = val[ixj];
+            val[ixj] = tv;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int q = 0; q < S; ++q) m = __dadd_rn(m, mis[q]);
+    solve_misfit[sd.gidx] = m;
+    int ns = 0;
+    long long cur = -1;
+    double acc = 0.0;
+    int64_t* sidx = A.seed_idx + sd.seed_off;
+    T* sval = A.seed_val + sd.seed_off;
+    for (int e = 0; e < P; ++e) {
+      const long long kk = key[e];
+      if (kk == LLONG_MAX) break;
+      const long long cell = kk >> 16;
+      if (cell != cur) {
+        if (cur >= 0) {
+          sidx[ns] = cur;
+          sval[ns] = (T)acc;
+          ++ns;
+        }
+        cur = cell;
+        acc = 0.0;
+      }
+      acc = __dadd_rn(acc, val[e]);
+    }
+    if (cur >= 0) {
+      sidx[ns] = cur;
+      sval[ns] = (T)acc;
+      ++ns;
+    }
+    A.n_seed[sd.gidx] = ns;
+  }
+}
+
+// ------------------------------------------------------------------ adjoint
+template <class T>
+__device__ __forceinline__ int upwind_side_t(const T* u, int64_t c, int pos, int ext, int64_t st,
+                                             T uc) {
+  int side;
+  T a;
+  if (pos == 0) {
+    side = 2;
+    a = u[c + st];
+  } else if (pos == ext - 1) {
+    side = 1;
+    a = u[c - st];
+  } else {
+    const T up = u[c + st], um = u[c - st];
+    if (up > um) {
+      side = 1;
+      a = um;
+    } else {
+      side = 2;
+      a = up;
+    }
+  }
+  return (uc > a) ? side : 0;
+}
+
+template <class T, int BK>
+__global__ void k_batch_adj(BatchArgs<T> A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_q;
+  __shared__ int s_changed;
+  const int NW = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr size_t WS = (2 * tile_elems(BK)) * sizeof(T) + itile_elems(BK) * sizeof(uint16_t);
+  T* U = reinterpret_cast<T*>(smem + warp * WS);
+  T* L = U + tile_elems(BK);
+  uint16_t* C = reinterpret_cast<uint16_t*>(L + tile_elems(BK));
+  unsigned long long cnt_upd = 0, cnt_brk = 0;
+  constexpr bool EXACT = sizeof(T) == 8;
+  for (;;) {
+    if (threadIdx.x == 0) s_q = atomicAdd(A.next, 1);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();
+    if (q >= A.n_solves) break;
+    const int gs = A.order[q];
+    const SolveDev sd = A.solves[gs];
+    const FieldDev<T> fd = A.fields[sd.field];
+    const Geom g = fd.g;
+    const T* u = A.u + sd.u_off;
+    T* lam = A.lam + sd.u_off;
+    uint16_t* code = A.code + sd.u_off;
+    const int nb = g.nbx * g.nby * g.nbz;
+    int* mod = A.meta + sd.meta_off;
+    int* proc = mod + nb;
+    const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+    // pass 1: upwind sides and fixed cells; lambda = 0
+    for (int64_t col = warp; col < (int64_t)g.m * g.n; col += NW) {
+      const int i = (int)(col / g.n), j = (int)(col % g.n);
+      for (int k = lane; k < g.l; k += 32) {
+        const int64_t c = col * g.l + k;
+        const T uc = u[c];
+        const int sx = upwind_side_t(u, c, i, g.m, sI, uc);
+        const int sy = upwind_side_t(u, c, j, g.n, sJ, uc);
+        const int sz = upwind_side_t(u, c, k, g.l, (int64_t)1, uc);
+        uint16_t cd = (uint16_t)(sx | (sy << 2) | (sz << 4));
+        if (uc == (T)u0_at(sd, i, j, k) || (sx | sy | sz) == 0) cd = CODE_FIXED;
+        code[c] = cd;
+        lam[c] = T(0);
+      }
+    }
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      mod[b] = -2;
+      proc[b] = -1;
+    }
+    __syncthreads();
+    // pass 2: users (reads only the low bits of neighbours, writes own high bits)
+    for (int64_t col = warp; col < (int64_t)g.m * g.n; col += NW) {
+      const int i = (int)(col / g.n), j = (int)(col % g.n);
+      for (int k = lane; k < g.l; k += 32) {
+        const int64_t c = col * g.l + k;
+        const uint16_t cd = code[c];
+        if (cd & CODE_FIXED) continue;
+        uint16_t us = 0;
+        auto uses = [&](int64_t r, int ax, int want) -> bool {
+          const uint16_t cr = code[r];
+          return !(cr & CODE_FIXED) && (((cr >> (2 * ax)) & 3) == want);
+        };
+        if (i > 0 && uses(c - sI, 0, 2)) us |= 1;
+        if (i < g.m - 1 && uses(c + sI, 0, 1)) us |= 2;
+        if (j > 0 && uses(c - sJ, 1, 2)) us |= 4;
+        if (j < g.n - 1 && uses(c + sJ, 1, 1)) us |= 8;
+        if (k > 0 && uses(c - 1, 2, 2)) us |= 16;
+        if (k < g.l - 1 && uses(c + 1, 2, 1)) us |= 32;
+        code[c] = (uint16_t)(cd | (us << CODE_USERS));
+      }
+    }
+    __syncthreads();
+    // seeds: mark cells and make their bricks dirty
+    const int ns = A.n_seed[sd.gidx];
+    const int64_t* sidx = A.seed_idx + sd.seed_off;
+    const T* sval = A.seed_val + sd.seed_off;
+    for (int e = threadIdx.x; e < ns; e += blockDim.x) {
+      const int64_t c = sidx[e];
+      const uint16_t cd = code[c];
+      if (cd & CODE_FIXED) continue;
+      code[c] = (uint16_t)(cd | CODE_SEED);
+      const int i = (int)(c / sI), j = (int)((c / sJ) % g.n), k = (int)(c % g.l);
+      mod[((i / BI) * g.nby + (j / BJ)) * g.nbz + (k / BK)] = -1;
+    }
+    __syncthreads();
+    int it;
+    bool conv = false;
+    for (it = 0; it < A.adj_max_iter; ++it) {
+      if (threadIdx.x == 0) s_changed = 0;
+      __syncthreads();
+      bool any = false;
+      for (int o = 0; o < 8; ++o) {
+        int si, sj, sk;
+        ordering3(o, si, sj, sk);
+        const int CS = tile_col_stride(BK, sj == sk);
+        for (int d = 0; d < g.nlev; ++d) {
+          const int t = (it * 8 + o) * g.nlev + d;
+          const int q1 = fd.lstart[d + 1];
+          for (int qq = fd.lstart[d] + warp; qq < q1; qq += NW) {
+            const BrickPos p = brick_pos<BK>(g, fd.bricks[qq], si, sj, sk);
+            if (!brick_needed(mod, proc, g, p, lane)) continue;
+            load_halo_tile<T, BK>(U, u, g, p, CS, lane);
+            load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
+            load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
+            cp_async_wait_all();
+            __syncwarp();
+            const bool ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g,
+                                                                 p, si, sj, sk, CS, lane);
+            if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+            __syncwarp();
+            if (lane == 0) {
+              const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
+              proc[b] = t;
+              if (ch) mod[b] = t;
+              cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
+              cnt_brk += 1;
+            }
+            any |= ch;
+          }
+          __syncthreads();
+        }
+      }
+      if (any && lane == 0) s_changed = 1;
+      __syncthreads();
+      const bool changed = s_changed != 0;
+      __syncthreads();
+      if (!changed) {
+        conv = true;
+        break;
+      }
+    }
+    if (threadIdx.x == 0) {
+      adt_solve_status& st = A.status[sd.gidx];
+      st.adj_iters = conv ? it + 1 : it;
+      st.adj_converged = conv ? 1 : 0;
+    }
+  }
+  if (lane == 0 && cnt_brk) {
+    atomicAdd(&A.counters[2], cnt_upd);
+    atomicAdd(&A.counters[3], cnt_brk);
+  }
+}
+
+// --------------------------------------------------------------- gradient
+// grad[c] += sum over the chunk's solves on this field (in solve order) of
+// -lambda_s[c] * (-2 f h h), in FP64 (Eikonal3D.cpp:163-166,244-246).
+template <class T>
+__global__ void k_batch_grad(const T* __restrict__ lam, const int64_t* __restrict__ u_off,
+                             int n_solves, const double* __restrict__ f64, double h, int64_t ncell,
+                             double* __restrict__ grad) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double rhs = __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f64[c]), h), h);
+    double G = grad[c];
+    for (int s = 0; s < n_solves; ++s) {
+      const double l = (double)lam[u_off[s] + c];
+      G = __dadd_rn(G, __dmul_rn(-l, rhs));
+    }
+    grad[c] = G;
+  }
+}
+
+}  // namespace adt

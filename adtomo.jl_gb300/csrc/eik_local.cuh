@@ -1,0 +1,80 @@
+// eik_local.cuh -- per-cell upwind updates.
+//
+// Two families:
+//  * *_exact (FP64): the reference's operation sequence written with IEEE
+//    round-to-nearest intrinsics (__dmul_rn, __dadd_rn, __ddiv_rn, __dsqrt_rn),
+//    which the compiler never contracts into FMAs, so results are bit-identical
+//    to the reference compiled for x86-64 (Eikonal.h:14-20, Eikonal3D.cpp:11-28).
+//  * upd3_stable<T>: the same roots written without the B^2 - 4C cancellation:
+//      two-term:   x = a + (d2 + sqrt(2 F^2 - d2^2)) / 2,           d2 = b - a
+//      three-term: x = a + (d2 + d3 + sqrt(3 F^2 - d2^2 - d3^2 - (d3-d2)^2)) / 3
+//    with F = f h.  Every term is a small difference, so FP32 keeps ~1 ulp of
+//    the travel time instead of losing digits to (a+b)^2 when u >> f h.
+#pragma once
+#include "adt_common.cuh"
+
+namespace adt {
+
+// Sorted three-term update, reference arithmetic (Eikonal3D.cpp:11-28).
+__device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, double f, double h) {
+  double t;
+  if (a1 > a2) { t = a1; a1 = a2; a2 = t; }
+  if (a1 > a3) { t = a1; a1 = a3; a3 = t; }
+  if (a2 > a3) { t = a2; a2 = a3; a3 = t; }
+  double x = __dadd_rn(a1, __dmul_rn(f, h));
+  if (x <= a2) return x;
+  const double ffhh = __dmul_rn(__dmul_rn(__dmul_rn(f, f), h), h);
+  double B = -__dadd_rn(a1, a2);
+  double C = __ddiv_rn(__dsub_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), ffhh), 2.0);
+  x = __ddiv_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 2.0);
+  if (x <= a3) return x;
+  B = __ddiv_rn(__dmul_rn(-2.0, __dadd_rn(__dadd_rn(a1, a2), a3)), 3.0);
+  C = __ddiv_rn(
+      __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), __dmul_rn(a3, a3)), ffhh),
+      3.0);
+  return __ddiv_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 2.0);
+}
+
+// Two-term update, reference arithmetic (Eikonal.h:14-20).
+__device__ __forceinline__ double upd2_exact(double a, double b, double f, double h) {
+  const double fh = __dmul_rn(f, h);
+  const double d = fabs(__dsub_rn(a, b));
+  if (d >= fh) return __dadd_rn(rmin(a, b), fh);
+  const double ab = __dsub_rn(a, b);
+  const double disc =
+      __dsub_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, f), f), h), h), __dmul_rn(ab, ab));
+  return __ddiv_rn(__dadd_rn(__dadd_rn(a, b), __dsqrt_rn(disc)), 2.0);
+}
+
+template <class T>
+__device__ __forceinline__ T tsqrt(T x);
+template <>
+__device__ __forceinline__ float tsqrt<float>(float x) {
+  return sqrtf(x);
+}
+template <>
+__device__ __forceinline__ double tsqrt<double>(double x) {
+  return sqrt(x);
+}
+
+// Cancellation-free sorted three-term update (same roots as upd3_exact).
+template <class T>
+__device__ __forceinline__ T upd3_stable(T a, T b, T c, T fh) {
+  T t;
+  if (a > b) { t = a; a = b; b = t; }
+  if (a > c) { t = a; a = c; c = t; }
+  if (b > c) { t = b; b = c; c = t; }
+  T x = a + fh;
+  if (x <= b) return x;
+  const T d2 = b - a;
+  const T F2 = fh * fh;
+  x = a + T(0.5) * (d2 + tsqrt<T>(T(2) * F2 - d2 * d2));
+  if (x <= c) return x;
+  const T d3 = c - a;
+  const T e = d3 - d2;
+  T disc = T(3) * F2 - d2 * d2 - d3 * d3 - e * e;
+  disc = disc > T(0) ? disc : T(0);
+  return a + (d2 + d3 + tsqrt<T>(disc)) * T(1.0 / 3.0);
+}
+
+}  // namespace adt

@@ -1,0 +1,295 @@
+"""Benchmark: forward + adjoint events/s on one GB300 (batched FP32).
+
+Workload (one "step" = one misfit + gradient evaluation): 256 events on one
+128 x 128 x 64 grid, h = 0.5 km, velocity rising linearly 4 -> 8 km/s with
+depth times a +-5% checkerboard of 8-cell blocks; sources uniform in the
+volume, 100 stations uniform on the top surface; observed times from a
++2%-noise velocity model.  Inputs are seeded synthetic data (the reference
+ships no dataset).  Each step: FP32 forward sweeps for all events, trilinear
+sampling + weighted misfit, FP32 adjoint sweeps, FP64 gradient summed over
+events.
+
+  value : events/s with inputs resident in HBM (CUDA events on the plan's
+          stream around K graph launches)
+  e2e   : events/s through adt_batch_run with host buffers (H2D of the
+          slowness and picks, D2H of misfit, predicted times, gradient and
+          status inside the timed region)
+  --impl reference : the reference's CPU algorithm (the oracle port of
+          Eikonal3D.cpp, all host threads) on a bounded sample of events.
+
+Under torchrun each rank runs the full 256-event workload on its own GPU
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "adtomo.jl_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+adjoint events/s on 1 GB300: batched FP32 vs plain FP64, ≤1e-4 rel error"
+M, N, L, H = 128, 128, 64, 0.5
+N_EVENTS, N_STA = 256, 100
+SEED = 0
+BYTES_PER_FWD_UPDATE = 12  # FP32: read u, read f, write u per cell-update
+BYTES_PER_ADJ_UPDATE = 16  # FP32: read u, read/write lambda, code (2 B) rounded
+
+
+def workload():
+    from adtomo_gb300 import synth
+    rng = np.random.default_rng(SEED)
+    f = synth.layered_checkerboard(M, N, L, block=8)
+    sta = synth.surface_stations(M, N, N_STA, rng)
+    src = synth.volume_sources(M, N, L, N_EVENTS, rng)
+    f_obs = f / (1.0 + 0.02 * rng.standard_normal(f.shape))
+    w = np.ones(N_EVENTS * N_STA)
+    return f, f_obs, sta, src, w
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 7:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons)}
+
+
+def cpu_events_per_s(sample_events, threads):
+    """The oracle port of the reference's CPU op on a bounded sample."""
+    from oracle import oracle as O
+    f, f_obs, sta, src, w = workload()
+    k = sample_events
+    t_obs = np.full(k * N_STA, 1.0)
+    t0 = time.perf_counter()
+    O.batch_misfit_grad([(f, H)], [sta], np.zeros(k, np.int32), src[:k], t_obs, w[:k * N_STA],
+                        tol=1e-6, max_iter=20, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return k / dt, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = max(threads, 16)
+    for _ in range(args.warmup):
+        cpu_events_per_s(min(sample, threads), threads)
+    vals, total = [], 0.0
+    for _ in range(args.steps):
+        v, dt = cpu_events_per_s(sample, threads)
+        vals.append(v)
+        total += dt
+    value = sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "C3: 256 events on 128x128x64, h=0.5 km, layered+checkerboard, "
+                               "100 surface stations", "sample_events_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} of the 256 events per step (oracle/eikonal_oracle.c, "
+                                   f"FP64, tol 1e-6, 20-iteration cap, {threads} threads)"},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import torch
+    import adtomo_gb300 as A
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    f, f_obs, sta, src, w = workload()
+    sf = np.zeros(N_EVENTS, np.int32)
+    B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6)
+    # observed times from the +2% noise model (setup, untimed)
+    B.upload([f_obs], np.full(N_EVENTS * N_STA, 1.0), w)
+    B.run_resident()
+    _, t_obs, _, _ = B.download()
+    B.upload([f], t_obs, w)
+    stream = torch.cuda.ExternalStream(B.stream())
+    for _ in range(args.warmup):
+        B.run_resident()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fwd_ms, adj_ms, upd_f, upd_a = [], [], [], []
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                B.run_resident()
+            end.record(stream)
+        torch.cuda.synchronize()
+        ms = start.elapsed_time(end)
+        st = B.stats()  # in-graph events of the last step
+        fwd_ms.append(st.fwd_ms)
+        adj_ms.append(st.adj_ms)
+        upd_f.append(st.fwd_cell_updates)
+        upd_a.append(st.adj_cell_updates)
+        # end to end through the C ABI with host buffers
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            mis, tp, grads, status = B.run([f], t_obs, w)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+    clocks = clk.summary()
+    t = torch.tensor([ms, e2e_s * 1000.0], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms, e2e_ms = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    ms_step = ms / args.steps
+    value = N_EVENTS * world / (ms_step / 1000.0)
+    e2e_val = N_EVENTS * world / (e2e_ms / 1000.0 / args.steps)
+    peak, peak_kind = peaks()
+    achieved = upd_f[-1] * BYTES_PER_FWD_UPDATE / (fwd_ms[-1] / 1000.0) / 1e9
+    n_obs = N_EVENTS * N_STA
+    h2d = M * N * L * 8 + 2 * n_obs * 8
+    d2h = 8 + n_obs * 8 + M * N * L * 8 + N_EVENTS * 24
+    ncu_traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_batch_fwd_c3_traffic.json")
+    if os.path.exists(prof):
+        try:
+            ncu_traffic = json.load(open(prof)).get("traffic_bytes_per_launch")
+        except (OSError, ValueError):
+            ncu_traffic = None
+    threads = os.cpu_count() or 1
+    cpu_sample = max(threads, 16) if args.cpu_sample is None else args.cpu_sample
+    cpu_val, cpu_dt = (cpu_events_per_s(cpu_sample, threads) if cpu_sample > 0 else (None, 0.0))
+    iters = [s.iters for s in status]
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded layered+checkerboard model)",
+        "config": {"workload": "C3: 256 events on 128x128x64, h=0.5 km, layered 4-8 km/s x "
+                               "(1+-5%) 8-cell checkerboard, 100 surface stations, misfit + "
+                               "summed slowness gradient",
+                   "events_per_gpu": N_EVENTS, "grid": [M, N, L], "l2": "inputs larger than L2 "
+                   "(1 GB of travel times + 1 GB of adjoint variables per step)",
+                   "bk": st.bk, "warps_per_cta": st.warps, "ctas": st.ctas,
+                   "fwd_iters_mean": float(np.mean(iters)),
+                   "adj_iters_mean": float(np.mean([s.adj_iters for s in status]))},
+        "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": ncu_traffic,
+                     "kernel": "k_batch_fwd (forward sweeps)", "peak_source": peak_kind,
+                     "bytes_per_update": BYTES_PER_FWD_UPDATE,
+                     "cell_updates_per_launch": int(upd_f[-1]), "launch_ms": fwd_ms[-1],
+                     "adjoint": {"launch_ms": adj_ms[-1], "cell_updates": int(upd_a[-1]),
+                                 "achieved_GBs": upd_a[-1] * BYTES_PER_ADJ_UPDATE /
+                                 (adj_ms[-1] / 1000.0) / 1e9}},
+        "cell_updates_per_s": (upd_f[-1] + upd_a[-1]) / (ms_step / 1000.0),
+        "cpu_baseline": ({"value": cpu_val, "unit": "events/s", "cores": threads, "kind": "port",
+                          "sample": f"{cpu_sample} of the 256 events (oracle port of "
+                                    f"Eikonal3D.cpp, FP64, tol 1e-6, 20-iteration cap), "
+                                    f"{cpu_dt:.1f} s"} if cpu_val else None),
+        "clocks": clocks,
+        "gpu_launches": 7 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    B.close()
+
+
+def main():
+    global N_EVENTS
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--events", type=int, default=N_EVENTS,
+                    help="events per GPU (default 256, the workload; smaller for profiling)")
+    ap.add_argument("--cpu-sample", type=int, default=None,
+                    help="events timed for the cpu_baseline (0 skips it)")
+    args = ap.parse_args()
+    N_EVENTS = args.events
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

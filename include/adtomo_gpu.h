@@ -1,0 +1,201 @@
+/*
+ * adtomo_gpu.h -- C ABI of the GB300 (sm_103a) Eikonal library libadtomo_gpu.so.
+ *
+ * Drop-in for the hot path of AI4EPS/ADTomo.jl: the TensorFlow custom ops
+ * Eikonal / EikonalGrad (deps/CustomOps/Eikonal/Eikonal.cpp) and
+ * EikonalThreeD / EikonalThreeDGrad (deps/CustomOps/Eikonal3D/EikonalThreeD.cpp),
+ * which the Julia functions eikonal(...) and eikonal3d(...) of
+ * src/eikonal_op.jl load through ADCME.load_op_and_grad.  A Julia caller binds
+ * these symbols with ccall; the Python package
+ * adtomo_gb300 binds them with ctypes.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Unless a function name ends in _device,
+ *    every array is HOST memory owned by the caller; results are on the host
+ *    when the call returns (the call is synchronous).
+ *  - Layouts are the ops' own flat layouts:
+ *      2D: (n+1) x (m+1) grid, index j*(m+1)+i   (Eikonal.h:30-48)
+ *      3D: m x n x l grid, C order, index i*n*l + j*l + k (Eikonal3D.cpp:6-8)
+ *    A column-major Julia Array (m,n,l) is passed as permutedims(A,(3,2,1)).
+ *  - Every function returns ADT_OK (0) or a negative ADT_E* code; the message
+ *    of the last error on the calling thread is adt_last_error().
+ *  - Inputs are validated before any device work (the reference's DCHECKs are
+ *    compiled out under -DNDEBUG; these checks replace them).
+ */
+#ifndef ADTOMO_GPU_H
+#define ADTOMO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADT_OK 0
+#define ADT_EINVAL (-1)    /* bad size, source index, non-finite or <= 0 slowness, ... */
+#define ADT_ENOMEM (-2)    /* device allocation failed */
+#define ADT_ECUDA (-3)     /* CUDA runtime error (message names the call) */
+#define ADT_ETIMEOUT (-4)  /* a bounded device wait ran out of its budget */
+#define ADT_ENOCONV (-5)   /* returned only when the caller asked for strict convergence */
+#define ADT_ESINGULAR (-6) /* 2D adjoint: a non-source cell has no upwind direction */
+#define ADT_ENODEV (-7)    /* no usable sm_103 device */
+
+/* Per-solve convergence record. */
+typedef struct adt_solve_status {
+  int32_t iters;     /* forward iterations (one iteration = all orderings) */
+  int32_t converged; /* 1 if the stopping rule was met before the iteration cap */
+  double final_err;  /* last stopping-rule value */
+  int32_t adj_iters; /* adjoint iterations (0 if no adjoint ran) */
+  int32_t adj_converged;
+} adt_solve_status;
+
+/* Message of the last error on the calling thread ("" if none). */
+const char* adt_last_error(void);
+/* Library version string. */
+const char* adt_version(void);
+/* Number of usable devices (0 when none); never fails. */
+int adt_device_count(void);
+
+/* ------------------------------------------------------------------------
+ * 2D op: replaces Eikonal (Eikonal.cpp:20-46, Compute :74-127).
+ * f: slowness, (n+1)*(m+1) doubles; srcx, srcy: 1-based source node (the op
+ * subtracts 1, Eikonal.cpp:125); h: grid spacing.  u: travel times out.
+ * FP64, bit-identical to the reference forward (Eikonal.h:54-93): 4 orderings,
+ * stop when ||u-u_old||/||u_old|| < 1e-8, at most 100 iterations.  A solve
+ * that hits the cap returns ADT_OK with status->converged = 0 (the reference
+ * prints "ERROR: Eikonal does not converge!", Eikonal.h:88-90).
+ * --------------------------------------------------------------------- */
+int adt_eikonal(const double* f, int64_t m, int64_t n, int64_t srcx, int64_t srcy, double h,
+                double* u, adt_solve_status* status);
+
+/* 2D gradient op: replaces EikonalGrad (Eikonal.cpp:48-63, Compute :141-221).
+ * Returns grad_f = dL/df for dL/du = grad_u at the converged u
+ * (Eikonal.h:95-200).  The other gradient outputs of the op are never written
+ * by the reference (Eikonal.cpp:187-211) and have no counterpart here. */
+int adt_eikonal_grad(const double* grad_u, const double* u, const double* f, int64_t m, int64_t n,
+                     int64_t srcx, int64_t srcy, double h, double* grad_f);
+
+/* Batched 2D forward: `count` independent solves on one slowness grid, source
+ * k at (srcx[k], srcy[k]) (1-based); u holds count*(n+1)*(m+1) doubles. */
+int adt_eikonal_batch(const double* f, int64_t m, int64_t n, int64_t count, const int64_t* srcx,
+                      const int64_t* srcy, double h, double* u, adt_solve_status* status);
+
+/* ------------------------------------------------------------------------
+ * 3D op: replaces EikonalThreeD (EikonalThreeD.cpp:14-45, Compute :77-140).
+ * u0: initial values (upper bounds), f: slowness, both m*n*l doubles; tol:
+ * stop when max|u-u_old| over an iteration < tol; at most 20 iterations as in
+ * the reference (Eikonal3D.cpp:71-88).  FP64, bit-identical to the reference.
+ * verbose != 0 prints the per-iteration error like the reference (:82-84).
+ * This is the plain single-solve path: one solve per call, FP64, no batching.
+ * --------------------------------------------------------------------- */
+int adt_eikonal_three_d(const double* u0, const double* f, double h, int64_t m, int64_t n,
+                        int64_t l, double tol, int verbose, double* u, adt_solve_status* status);
+
+/* 3D gradient op: replaces EikonalThreeDGrad (EikonalThreeD.cpp:47-65,
+ * Compute :154-250; math Eikonal3D.cpp:96-198).  grad_u0 = grad_u where
+ * u == u0 exactly (else 0); grad_f = 2 f h^2 lambda with A^T lambda = grad_u
+ * solved by reverse causal sweeps.  tol and verbose are accepted for
+ * signature parity and unused, as in the reference. */
+int adt_eikonal_three_d_grad(const double* grad_u, const double* u, const double* u0,
+                             const double* f, double h, int64_t m, int64_t n, int64_t l,
+                             double tol, int verbose, double* grad_u0, double* grad_f);
+
+/* Same two ops on DEVICE pointers, enqueued on `stream` (a cudaStream_t, or
+ * NULL for the default stream).  The call returns after the work completes. */
+int adt_eikonal_three_d_device(const double* u0, const double* f, double h, int64_t m, int64_t n,
+                               int64_t l, double tol, int verbose, double* u,
+                               adt_solve_status* status, void* stream);
+int adt_eikonal_three_d_grad_device(const double* grad_u, const double* u, const double* u0,
+                                    const double* f, double h, int64_t m, int64_t n, int64_t l,
+                                    double* grad_u0, double* grad_f, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Batched misfit + slowness gradient: the per-evaluation loop of
+ * scripts/inversion.jl:46-105 (per-source eikonal3d, trilinear sampling at
+ * receivers, weighted L2 misfit with missing picks, gradient) for many
+ * sources and several fields (P and S, grids of different size) in one plan.
+ *
+ *   fields f = 0..n_fields-1: dims[3f..3f+2] = (m,n,l), h[f], nsta[f]
+ *       receivers at sta_xyz (3 doubles each, fractional 0-based node
+ *       coordinates, concatenated over fields)
+ *   solves s = 0..n_solves-1: field solve_field[s], source src_xyz[3s..3s+2]
+ *       (fractional 0-based node coordinates).  u0 is 1000 everywhere except
+ *       the 8 nodes around the source, which get dist * f * h computed in FP64
+ *       (scripts/gene_obs.jl:44-51); no gradient flows through u0, as in
+ *       scripts/inversion.jl where u0 is built from vel0.
+ *   picks: t_obs and weight, nsta[solve_field[s]] per solve, concatenated;
+ *       t_obs == -1 marks a missing pick (scripts/inversion.jl:81).
+ *   outputs: misfit = sum weight*(t_obs - t_pred)^2, t_pred (like t_obs),
+ *       grad (concatenated fields, m*n*l doubles each) summed over solves in
+ *       FP64, status per solve.
+ * --------------------------------------------------------------------- */
+#define ADT_F32 0
+#define ADT_F64 1
+
+typedef struct adt_batch_opts {
+  int32_t precision;    /* ADT_F32 (default) or ADT_F64 */
+  double tol;           /* forward stop: max travel-time decrease in an iteration < tol (s) */
+  int32_t max_iter;     /* forward iteration cap (default 200) */
+  int32_t adj_max_iter; /* adjoint iteration cap (default 200) */
+  int32_t ref_compat;   /* 1: reference stopping rule max|u-u_old| and cap 20 (F64 only) */
+  int32_t near_src_f64; /* FP32: cells within this Chebyshev distance of the source
+                           box update in FP64 (default 2; -1 disables) */
+  int32_t chunk;        /* solves resident at once; forward fields are recomputed
+                           per chunk (0 = all solves at once) */
+  int32_t bk;           /* brick depth along k: 0 = autotune, else 32 or 64 */
+  int32_t warps;        /* warps per CTA: 0 = autotune */
+  int32_t use_graph;    /* 1 (default): replay the evaluation as a CUDA graph */
+} adt_batch_opts;
+
+typedef struct adt_batch adt_batch;
+
+void adt_batch_opts_default(adt_batch_opts* opts);
+
+int adt_batch_create(adt_batch** out, int32_t n_fields, const int32_t* dims, const double* h,
+                     const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
+                     const int32_t* solve_field, const double* src_xyz,
+                     const adt_batch_opts* opts);
+int adt_batch_destroy(adt_batch* b);
+
+/* One evaluation end to end: host inputs are copied to the device, the
+ * evaluation runs, host outputs are written.  slowness: concatenated fields
+ * (doubles); t_obs/weight as described above.  Any output pointer may be NULL. */
+int adt_batch_run(adt_batch* b, const double* slowness, const double* t_obs, const double* weight,
+                  double* misfit, double* t_pred, double* grad, adt_solve_status* status);
+
+/* Device-resident use: upload inputs once, run, read outputs later.  upload
+ * takes host pointers (NULL leaves that input unchanged); run_resident enqueues
+ * one evaluation on the plan's stream without synchronising; download copies
+ * outputs to host pointers (NULL skips) after synchronising. */
+int adt_batch_upload(adt_batch* b, const double* slowness, const double* t_obs,
+                     const double* weight);
+int adt_batch_run_resident(adt_batch* b);
+int adt_batch_download(adt_batch* b, double* misfit, double* t_pred, double* grad,
+                       adt_solve_status* status);
+/* The plan's cudaStream_t (for event timing by the caller). */
+void* adt_batch_stream(adt_batch* b);
+/* Device pointers of the plan's resident buffers (for zero-copy callers):
+ * which = 0 slowness (F64), 1 grad (F64), 2 t_pred (F64), 3 misfit (F64, 1). */
+void* adt_batch_device_buffer(adt_batch* b, int32_t which);
+/* Counters of the last evaluation: cell updates performed by the forward and
+ * the adjoint sweeps, bricks processed, and device times in ms of the
+ * forward sweep, adjoint sweep, and whole evaluation (measured with CUDA
+ * events on the plan's stream; -1 when unavailable). */
+typedef struct adt_batch_stats {
+  int64_t fwd_cell_updates;
+  int64_t adj_cell_updates;
+  int64_t fwd_bricks;
+  int64_t adj_bricks;
+  float fwd_ms;
+  float adj_ms;
+  float total_ms;
+  int32_t bk;
+  int32_t warps;
+  int32_t ctas;
+} adt_batch_stats;
+int adt_batch_stats_get(adt_batch* b, adt_batch_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

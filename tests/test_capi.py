@@ -1,0 +1,78 @@
+"""The C-ABI library: it loads, exports every symbol the header declares, and
+rejects invalid input before any device work (CPU only, no GPU needed)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import adtomo_gb300 as A
+from adtomo_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "adtomo_gpu.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(adt_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = A.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) == set(_lib.SIGNATURES), "ctypes signatures must cover the header exactly"
+
+
+def test_version_and_device_count_do_not_fail():
+    L = A.lib()
+    assert b"sm_103a" in L.adt_version()
+    assert L.adt_device_count() >= 0
+
+
+@pytest.mark.parametrize("dims", [(1, 4, 4), (4, 1, 4), (4, 4, 1), (0, 3, 3)])
+def test_eikonal3d_rejects_small_grids(dims):
+    m, n, l = dims
+    with pytest.raises(A.AdtError) as e:
+        A.eikonal3d(np.zeros(max(m * n * l, 1)), np.ones(max(m * n * l, 1)), 1.0, m, n, l, 1e-6)
+    assert e.value.code == -1
+
+
+def test_eikonal3d_rejects_bad_slowness_and_h():
+    u0 = np.full(27, 1000.0)
+    f = np.ones(27)
+    f[5] = -1.0
+    with pytest.raises(A.AdtError) as e:
+        A.eikonal3d(u0, f, 1.0, 3, 3, 3, 1e-6)
+    assert e.value.code == -1
+    f[5] = np.nan
+    with pytest.raises(A.AdtError):
+        A.eikonal3d(u0, f, 1.0, 3, 3, 3, 1e-6)
+    with pytest.raises(A.AdtError):
+        A.eikonal3d(u0, np.ones(27), 0.0, 3, 3, 3, 1e-6)
+    with pytest.raises(A.AdtError):
+        A.eikonal3d(u0, np.ones(27), 1.0, 3, 3, 3, -1.0)
+
+
+def test_eikonal2d_rejects_source_outside():
+    f = np.ones((5, 7))
+    for sx, sy in [(0, 1), (8, 1), (1, 0), (1, 6)]:
+        with pytest.raises(A.AdtError) as e:
+            A.eikonal(f, sx, sy, 1.0)
+        assert e.value.code == -1
+
+
+def test_size_mismatch_is_rejected_host_side():
+    with pytest.raises(A.AdtError):
+        A.eikonal3d(np.zeros(10), np.ones(10), 1.0, 3, 3, 3, 1e-6)
+
+
+@pytest.mark.skipif(A.lib().adt_device_count() > 0, reason="a GPU is present")
+def test_valid_call_without_gpu_reports_nodev():
+    with pytest.raises(A.AdtError) as e:
+        A.eikonal3d(np.full(27, 1000.0), np.ones(27), 1.0, 3, 3, 3, 1e-6)
+    assert e.value.name == "ADT_ENODEV"

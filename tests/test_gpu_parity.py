@@ -1,0 +1,277 @@
+"""GPU parity: the CUDA library through its C ABI against the oracle.
+
+Tolerances (stated per test):
+  * plain FP64 path (adt_eikonal, adt_eikonal_three_d): travel times
+    bit-identical to the oracle and to the reference golden vectors; adjoint
+    bit-identical to the oracle (same per-cell formula and summation order)
+    and within 1e-12 relative of the reference's SparseLU solution.
+  * batched FP64 with the reference stopping rule: misfit, predicted times and
+    summed gradient bit-identical to the oracle's batch.
+  * batched FP32: relative travel-time error <= 1e-4 (max over picks) and
+    relative gradient error <= 1e-3 (L2 norm) against the FP64 oracle.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import adtomo_gb300 as A
+from adtomo_gb300 import synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def need_gpu():
+    if A.lib().adt_device_count() < 1:
+        pytest.skip("no GPU")
+
+
+def rel_max(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+# ------------------------------------------------------------ golden ----
+@pytest.mark.parametrize("path", GOLD, ids=[os.path.basename(p)[:-4] for p in GOLD])
+def test_plain_fp64_matches_reference_golden(path):
+    g = np.load(path)
+    if str(g["kind"]) == "2d":
+        ix, jx, h = int(g["ix"]), int(g["jx"]), float(g["h"])
+        u = A.eikonal(g["f"], ix + 1, jx + 1, h)
+        assert np.array_equal(u, g["u"])
+        gf = A.eikonal_grad(g["grad_u"], g["u"], g["f"], ix + 1, jx + 1, h)
+        assert rel_max(gf, g["grad_f"]) <= 1e-12
+        assert np.array_equal(gf, O.eik2d_backward(g["grad_u"], g["u"], g["f"], ix, jx, h))
+    else:
+        m, n, l = g["f"].shape
+        h, tol = float(g["h"]), float(g["tol"])
+        u = A.eikonal3d(g["u0"], g["f"], h, m, n, l, tol)
+        assert np.array_equal(u, g["u"])
+        g0, gf = A.eikonal3d_grad(g["grad_u"], g["u"], g["u0"], g["f"], h, m, n, l)
+        assert np.array_equal(g0, g["grad_u0"])
+        assert rel_max(gf, g["grad_f"]) <= 1e-12
+        r0, rf = O.eik3d_backward(g["grad_u"], g["u"], g["u0"], g["f"], h)
+        assert np.array_equal(gf, rf)
+
+
+# ------------------------------------------------- plain FP64, seeded ----
+CASES3 = [
+    # (m, n, l, source) -- ragged extents, k longer than a brick, tiny grids
+    (9, 13, 37, (4.5, 6.2, 17.9)),
+    (17, 6, 70, (0.0, 0.0, 0.0)),
+    (2, 2, 2, (1.0, 0.0, 1.0)),
+    (33, 5, 3, (32.0, 4.0, 2.0)),
+    (24, 20, 66, (11.7, 3.1, 64.6)),
+]
+
+
+@pytest.mark.parametrize("case", CASES3, ids=[f"{c[0]}x{c[1]}x{c[2]}" for c in CASES3])
+def test_plain_fp64_random_models(case):
+    m, n, l, src = case
+    rng = np.random.default_rng(m * 1000 + n * 10 + l)
+    f = rng.uniform(0.15, 0.35, size=(m, n, l))
+    h = 0.5
+    u0 = O.src_u0(f, h, src)
+    u, st = A.eikonal3d(u0, f, h, m, n, l, 1e-9, return_status=True)
+    ur, it, _ = O.eik3d_forward(u0, f, h, 1e-9)
+    assert np.array_equal(u, ur)
+    assert st.iters == it
+    gu = rng.standard_normal((m, n, l))
+    g0, gf = A.eikonal3d_grad(gu, u, u0, f, h, m, n, l)
+    r0, rf = O.eik3d_backward(gu, ur, u0, f, h)
+    assert np.array_equal(g0, r0)
+    assert np.array_equal(gf, rf)
+
+
+def test_plain_fp64_iteration_cap_and_status():
+    m, n, l = 20, 18, 16
+    f = synth.layered_checkerboard(m, n, l, block=4)
+    u0 = O.src_u0(f, 1.0, (10.2, 9.1, 8.3))
+    u, st = A.eikonal3d(u0, f, 1.0, m, n, l, 0.0, return_status=True)
+    ur, it, err = O.eik3d_forward(u0, f, 1.0, 0.0, 20)
+    assert it == 20 and st.iters == 20 and st.converged == 0
+    assert np.array_equal(u, ur)
+    assert st.final_err == err
+
+
+def test_c2_config_fp64_forward_adjoint_and_fd():
+    """64x64x32, h=1 km, layered 4->8 km/s x (1 +- 5%) checkerboard of 8-cell
+    blocks, random interior source, 50 receivers on the top surface; central
+    finite differences (delta = 1e-6 f) on 20 random cells agree with the
+    adjoint gradient to 1e-4 relative."""
+    rng = np.random.default_rng(1)
+    m, n, l, h = 64, 64, 32, 1.0
+    f = synth.layered_checkerboard(m, n, l, block=8)
+    src = synth.volume_sources(m, n, l, 1, rng)[0]
+    sta = synth.surface_stations(m, n, 50, rng)
+    u0 = O.src_u0(f, h, src)
+    tol = 0.0
+    u = A.eikonal3d(u0, f, h, m, n, l, tol)
+    ur, _, _ = O.eik3d_forward(u0, f, h, tol)
+    assert np.array_equal(u, ur)
+    f_obs = f * (1 + 0.02 * rng.standard_normal(f.shape))
+    uo = A.eikonal3d(O.src_u0(f_obs, h, src), f_obs, h, m, n, l, tol)
+    t_obs = np.array([O.sample(uo, s)[0] for s in sta])
+
+    def misfit(uu):
+        return sum((t_obs[q] - O.sample(uu, sta[q])[0]) ** 2 for q in range(len(sta)))
+
+    gu = np.zeros_like(u)
+    for q in range(len(sta)):
+        t, idx, w = O.sample(u, sta[q])
+        np.add.at(gu.ravel(), idx, -2 * (t_obs[q] - t) * w)
+    _, gf = A.eikonal3d_grad(gu, u, u0, f, h, m, n, l)
+    _, rf = O.eik3d_backward(gu, ur, u0, f, h)
+    assert np.array_equal(gf, rf)
+    # FD on 20 random cells with non-negligible sensitivity (u0 held fixed).
+    # With delta = 1e-6 f the FD quotient carries ~1e-4 relative round-off
+    # (one ulp of a ~10 s travel time over a ~1e-10 misfit change), so it is
+    # checked to 1e-3; delta = 1e-4 f is checked to 1e-5.
+    cand = np.flatnonzero((np.abs(gf.ravel()) > 1e-3 * np.abs(gf).max()) & (u0.ravel() >= 1000))
+    cells = rng.choice(cand, size=20, replace=False)
+    for c in cells:
+        for rel, tol_fd in ((1e-6, 1e-3), (1e-4, 1e-5)):
+            d = rel * f.ravel()[c]
+            fp = f.copy().ravel()
+            fp[c] += d
+            fm = f.copy().ravel()
+            fm[c] -= d
+            # tol 0: all 20 iterations, so both solves sit on their fixed points
+            up = A.eikonal3d(u0, fp.reshape(f.shape), h, m, n, l, 0.0)
+            um = A.eikonal3d(u0, fm.reshape(f.shape), h, m, n, l, 0.0)
+            fd = (misfit(up) - misfit(um)) / (2 * d)
+            g = gf.ravel()[c]
+            assert abs(fd - g) <= tol_fd * abs(g), (c, rel, fd, g)
+
+
+def test_2d_c1_config_forward_and_grad():
+    """101x101, h=1, 6 km/s with 3 Gaussian anomalies, interior source, L2
+    misfit at 20 receivers against times from a +2%-noise velocity."""
+    rng = np.random.default_rng(2)
+    v = synth.gaussian_anomalies_2d(101, 101, rng)
+    f = 1.0 / v
+    ix, jx = (int(x) for x in rng.integers(5, 96, size=2))
+    u, st = A.eikonal(f, ix + 1, jx + 1, 1.0, return_status=True)
+    ur, it, conv = O.eik2d_forward(f, ix, jx, 1.0)
+    assert np.array_equal(u, ur) and st.iters == it and st.converged == conv
+    f_obs = 1.0 / (v * (1 + 0.02 * rng.standard_normal(v.shape)))
+    uo = A.eikonal(f_obs, ix + 1, jx + 1, 1.0)
+    rec = rng.integers(0, 101, size=(20, 2))
+    gu = np.zeros_like(u)
+    for r in rec:
+        gu[r[0], r[1]] += -2 * (uo[r[0], r[1]] - u[r[0], r[1]])
+    gf = A.eikonal_grad(gu, u, f, ix + 1, jx + 1, 1.0)
+    assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 1.0))
+
+
+def test_2d_batch_matches_single_solves():
+    rng = np.random.default_rng(4)
+    f = rng.uniform(0.5, 1.5, size=(23, 31))
+    sx = rng.integers(1, 32, size=5)
+    sy = rng.integers(1, 24, size=5)
+    u, st = A.eikonal_batch(f, sx, sy, 0.7)
+    for k in range(5):
+        ur, it, conv = O.eik2d_forward(f, sx[k] - 1, sy[k] - 1, 0.7)
+        assert np.array_equal(u[k], ur)
+        assert st[k] == (it, int(conv))
+
+
+# --------------------------------------------------------- batched ------
+def make_batch(rng, fields_dims, n_src, n_sta, missing=0.1):
+    fields, stations, slow = [], [], []
+    for (m, n, l, h) in fields_dims:
+        fields.append((m, n, l, h))
+        slow.append(synth.layered_checkerboard(m, n, l, block=4))
+        sta = synth.surface_stations(m, n, n_sta, rng)
+        sta[0] = [0.0, 0.0, 0.0]  # integer position: x1 == x2 branches
+        sta[1] = [m - 1, 2.5, 0.0]
+        stations.append(sta)
+    solve_field, src = [], []
+    for s in range(n_src):
+        fi = s % len(fields_dims)
+        m, n, l, _ = fields_dims[fi]
+        solve_field.append(fi)
+        src.append(synth.volume_sources(m, n, l, 1, rng)[0])
+    src[0] = [0.0, 0.0, 0.0]  # a corner source
+    n_obs = sum(len(stations[fi]) for fi in solve_field)
+    t_obs = rng.uniform(0.5, 3.0, n_obs)
+    t_obs[rng.random(n_obs) < missing] = -1.0
+    w = rng.uniform(0.5, 1.0, n_obs)
+    w[3] = 0.0
+    return fields, stations, slow, np.array(solve_field), np.array(src), t_obs, w
+
+
+def oracle_batch(fields, stations, slow, sf, src, t_obs, w, tol, max_iter):
+    return O.batch_misfit_grad([(s, f[3]) for s, f in zip(slow, fields)], stations, sf, src, t_obs,
+                               w, tol=tol, max_iter=max_iter)
+
+
+def test_batch_fp64_ref_compat_bit_exact():
+    rng = np.random.default_rng(7)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(20, 17, 13, 0.5), (12, 26, 40, 0.25)], 6, 9)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, ito = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-6, 20)
+    assert np.array_equal(tp, tpo)
+    assert mis == mo
+    for g, r in zip(grads, go):
+        assert np.array_equal(g, r)
+    assert [s.iters for s in st] == list(ito)
+    B.close()
+
+
+def test_batch_fp32_accuracy_against_fp64():
+    rng = np.random.default_rng(8)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(40, 36, 24, 0.5), (24, 24, 48, 0.5)], 8, 12)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4
+    assert abs(mis - mo) <= 1e-3 * mo
+    for g, r in zip(grads, go):
+        assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
+    assert all(s.converged and s.adj_converged for s in st)
+    B.close()
+
+
+def test_batch_chunking_and_graph_do_not_change_results():
+    rng = np.random.default_rng(9)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 7, 6)
+    ref = A.Batch3D(fields, stations, sf, src, use_graph=False)
+    r = ref.run(slow, t_obs, w)
+    for kw in ({"chunk": 3}, {"chunk": 1, "use_graph": True}, {"bk": 64}, {"warps": 3}):
+        B = A.Batch3D(fields, stations, sf, src, **kw)
+        out = B.run(slow, t_obs, w)
+        assert out[0] == r[0], kw
+        assert np.array_equal(out[1], r[1]), kw
+        assert np.array_equal(out[2][0], r[2][0]), kw
+        # a second evaluation of the same plan reproduces the first
+        out2 = B.run(slow, t_obs, w)
+        assert np.array_equal(out2[2][0], out[2][0]), kw
+        B.close()
+    ref.close()
+
+
+def test_batch_nonconvergence_is_reported():
+    rng = np.random.default_rng(10)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(30, 30, 20, 0.5)], 2, 5)
+    B = A.Batch3D(fields, stations, sf, src, max_iter=1, adj_max_iter=1)
+    _, _, _, st = B.run(slow, t_obs, w)
+    assert all(s.iters == 1 and s.converged == 0 for s in st)
+    B.close()
+
+
+def test_batch_rejects_bad_geometry():
+    with pytest.raises(A.AdtError):
+        A.Batch3D([(10, 10, 10, 1.0)], [np.array([[11.0, 0.0, 0.0]])], [0], [[1.0, 1.0, 1.0]])
+    with pytest.raises(A.AdtError):
+        A.Batch3D([(10, 10, 10, 1.0)], [np.zeros((1, 3))], [0], [[-0.5, 1.0, 1.0]])
+    with pytest.raises(A.AdtError):
+        A.Batch3D([(10, 10, 10, 1.0)], [np.zeros((1, 3))], [1], [[1.0, 1.0, 1.0]])
