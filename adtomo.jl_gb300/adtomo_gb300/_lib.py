@@ -41,14 +41,14 @@ class BatchOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("tol", C.c_double), ("max_iter", C.c_int32),
                 ("adj_max_iter", C.c_int32), ("ref_compat", C.c_int32),
                 ("near_src_f64", C.c_int32), ("chunk", C.c_int32), ("bk", C.c_int32),
-                ("warps", C.c_int32), ("use_graph", C.c_int32)]
+                ("warps", C.c_int32), ("groups", C.c_int32), ("use_graph", C.c_int32)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("fwd_cell_updates", C.c_int64), ("adj_cell_updates", C.c_int64),
                 ("fwd_bricks", C.c_int64), ("adj_bricks", C.c_int64), ("fwd_ms", C.c_float),
                 ("adj_ms", C.c_float), ("total_ms", C.c_float), ("bk", C.c_int32),
-                ("warps", C.c_int32), ("ctas", C.c_int32)]
+                ("warps", C.c_int32), ("groups", C.c_int32), ("ctas", C.c_int32)]
 
 
 _P = C.c_void_p

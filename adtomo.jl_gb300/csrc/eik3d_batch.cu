@@ -132,6 +132,8 @@ struct BatchPlan {
   // launch shapes
   KernelSet ks;
   int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
+  int fwd_gw = 4, fwd_groups = 2, adj_gw = 2, adj_groups = 4;
+  int max_nb = 0, meta_smem = 0;
   size_t fwd_smem = 0, adj_smem = 0, mis_smem = 0;
   // graph and timing
   cudaGraphExec_t graph = nullptr;
@@ -155,10 +157,11 @@ void batch_opts_default(adt_batch_opts* o) {
   o->chunk = 0;
   o->bk = 0;
   o->warps = 0;
+  o->groups = 0;
   o->use_graph = 1;
 }
 
-static int enqueue(BatchPlan& P);
+static int enqueue(BatchPlan& P, bool capturing);
 
 int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* hh,
                  const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
@@ -192,7 +195,8 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       return set_error(ADT_EINVAL, "batch: field %d has %d receivers (0..1024 supported)", f, nsta[f]);
     minl = std::min(minl, l);
   }
-  P->bk = o.bk ? o.bk : (minl >= 48 ? 64 : 32);
+  (void)minl;
+  P->bk = o.bk ? o.bk : 32;
   P->nf = n_fields;
   int64_t sofs = 0;
   for (int f = 0; f < n_fields; ++f) {
@@ -369,30 +373,59 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     ADT_CUDA(cudaMemcpy(P->d_order.p, ord.data(), ord.size() * 4, cudaMemcpyHostToDevice));
     if (!uo.empty()) ADT_CUDA(cudaMemcpy(P->d_uoff.p, uo.data(), uo.size() * 8, cudaMemcpyHostToDevice));
   }
-  // launch shapes: as many warps (bricks in flight) as shared memory allows
+  // launch shapes: warp groups (one solve each) per CTA, as many as fit
   int sm_count = 0, smem_optin = 0;
   ADT_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, P->dev));
   ADT_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->dev));
   const size_t budget = (size_t)smem_optin - 1024;
   const size_t fw = P->f64 ? fwd_warp_smem<double>(P->bk) : fwd_warp_smem<float>(P->bk);
   const size_t aw = P->f64 ? adj_warp_smem<double>(P->bk) : adj_warp_smem<float>(P->bk);
-  P->fwd_warps = (int)std::min<size_t>(16, budget / fw);
-  P->adj_warps = (int)std::min<size_t>(16, budget / aw);
-  if (o.warps > 0) {
-    P->fwd_warps = std::min(P->fwd_warps, (int)o.warps);
-    P->adj_warps = std::min(P->adj_warps, (int)o.warps);
-  }
-  if (P->fwd_warps < 1 || P->adj_warps < 1)
-    return set_error(ADT_EINVAL, "batch: brick tile does not fit in shared memory");
-  P->fwd_smem = P->fwd_warps * fw;
-  P->adj_smem = P->adj_warps * aw;
+  for (auto& g : P->geoms) P->max_nb = std::max(P->max_nb, g.nbx * g.nby * g.nbz);
+  P->meta_smem = (2 * (size_t)P->max_nb * sizeof(int) <= 16384) ? 1 : 0;
+  cudaFuncAttributes fa_f, fa_a;
+  ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
+  ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
+  auto shape = [&](size_t warp_bytes, int gw_default, int regs, int& gw, int& groups) -> int {
+    const int max_warps = std::min(32, 65536 / std::max(1, regs * 32));
+    gw = o.warps > 0 ? o.warps : gw_default;
+    gw = std::min(gw, max_warps);
+    for (;;) {
+      int G = 1;
+      while (G < 15 && group_hdr_bytes(G + 1, P->meta_smem, P->max_nb) + (size_t)(G + 1) * gw * warp_bytes <= budget &&
+             (G + 1) * gw <= max_warps)
+        ++G;
+      if (group_hdr_bytes(G, P->meta_smem, P->max_nb) + (size_t)G * gw * warp_bytes <= budget) {
+        if (o.groups > 0) G = std::min(G, (int)o.groups);
+        groups = G;
+        return ADT_OK;
+      }
+      if (gw == 1) return set_error(ADT_EINVAL, "batch: brick tile does not fit in shared memory");
+      --gw;
+    }
+  };
+  if ((rc = shape(fw, P->f64 ? 2 : 4, fa_f.numRegs, P->fwd_gw, P->fwd_groups))) return rc;
+  if ((rc = shape(aw, P->f64 ? 2 : 4, fa_a.numRegs, P->adj_gw, P->adj_groups))) return rc;
+  // verify with the occupancy calculator; shrink until one CTA fits
+  auto fits = [&](const void* fn, int gw, int& groups, size_t warp_bytes, size_t& smem) -> int {
+    for (;;) {
+      smem = group_hdr_bytes(groups, P->meta_smem, P->max_nb) + (size_t)groups * gw * warp_bytes;
+      ADT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int occ = 0;
+      ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, groups * gw * 32, smem));
+      if (occ >= 1) return ADT_OK;
+      if (groups == 1) return set_error(ADT_EINVAL, "batch: no launch shape fits on this device");
+      --groups;
+    }
+  };
+  if ((rc = fits(P->ks.fwd, P->fwd_gw, P->fwd_groups, fw, P->fwd_smem))) return rc;
+  if ((rc = fits(P->ks.adj, P->adj_gw, P->adj_groups, aw, P->adj_smem))) return rc;
+  P->fwd_warps = P->fwd_gw * P->fwd_groups;
+  P->adj_warps = P->adj_gw * P->adj_groups;
   int maxsta = 0;
   for (int f = 0; f < n_fields; ++f) maxsta = std::max(maxsta, P->nsta[f]);
   int pw = 1;
   while (pw < 8 * maxsta) pw <<= 1;
   P->mis_smem = (size_t)pw * 16 + (size_t)maxsta * 8 + 16;
-  ADT_CUDA(cudaFuncSetAttribute(P->ks.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->fwd_smem));
-  ADT_CUDA(cudaFuncSetAttribute(P->ks.adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->adj_smem));
   ADT_CUDA(cudaFuncSetAttribute(P->ks.misfit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->mis_smem));
   int occ_f = 0, occ_a = 0;
   ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, P->ks.fwd, P->fwd_warps * 32, P->fwd_smem));
@@ -403,7 +436,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     int64_t maxc = 0;
     for (auto& g : P->geoms) maxc = std::max(maxc, g.ncell);
     P->snap_stride = maxc;
-    R_(P->d_snap, (size_t)maxc * es * P->fwd_ctas);
+    R_(P->d_snap, (size_t)maxc * es * P->fwd_ctas * P->fwd_groups);
   }
 #undef R_
   P->ev.resize(4 * P->chunks.size() + 2);
@@ -438,12 +471,17 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.adj_max_iter = P.opts.adj_max_iter;
   A.ref_compat = P.opts.ref_compat;
   A.near_r = P.opts.near_src_f64;
+  A.group_warps = which_counter % 2 == 0 ? P.fwd_gw : P.adj_gw;
+  A.meta_smem = P.meta_smem;
+  A.max_nb = P.max_nb;
   return A;
 }
 
 template <class T>
-static int enqueue_t(BatchPlan& P) {
+static int enqueue_t(BatchPlan& P, bool capturing) {
   cudaStream_t st = P.stream;
+  // inside a graph capture the timing events must be external event nodes
+  const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (!P.f64)
     k_to_t_f32<<<grid1d(P.ncell_total), 256, 0, st>>>(P.d_slow64.as<double>(), P.d_slowT.as<float>(),
                                                       P.ncell_total);
@@ -452,19 +490,19 @@ static int enqueue_t(BatchPlan& P) {
   ADT_CUDA(cudaMemsetAsync(P.d_grad.p, 0, P.ncell_total * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_next.p, 0, 2 * P.chunks.size() * 4, st));
-  ADT_CUDA(cudaEventRecord(P.ev[4 * P.chunks.size()], st));
+  ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * P.chunks.size()], st, evf));
   for (size_t c = 0; c < P.chunks.size(); ++c) {
     const auto& ch = P.chunks[c];
     BatchArgs<T> Af = make_args<T>(P, ch, (int)(2 * c));
     BatchArgs<T> Aa = make_args<T>(P, ch, (int)(2 * c + 1));
     const int gf = std::min(P.fwd_ctas, ch.count);
     const int ga = std::min(P.adj_ctas, ch.count);
-    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 0], st));
+    ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 0], st, evf));
     {
       void* args[] = {&Af};
       ADT_CUDA(cudaLaunchKernel(P.ks.fwd, dim3(gf), dim3(P.fwd_warps * 32), args, P.fwd_smem, st));
     }
-    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 1], st));
+    ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 1], st, evf));
     {
       const double* tobs = P.d_tobs.as<double>();
       const double* w = P.d_w.as<double>();
@@ -473,12 +511,12 @@ static int enqueue_t(BatchPlan& P) {
       void* args[] = {&Af, &tobs, &w, &tp, &sm};
       ADT_CUDA(cudaLaunchKernel(P.ks.misfit, dim3(ch.count), dim3(256), args, P.mis_smem, st));
     }
-    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 2], st));
+    ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 2], st, evf));
     {
       void* args[] = {&Aa};
       ADT_CUDA(cudaLaunchKernel(P.ks.adj, dim3(ga), dim3(P.adj_warps * 32), args, P.adj_smem, st));
     }
-    ADT_CUDA(cudaEventRecord(P.ev[4 * c + 3], st));
+    ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 3], st, evf));
     for (int f = 0; f < P.nf; ++f) {
       const int cnt = (int)ch.field_uoff[f].size();
       if (!cnt) continue;
@@ -494,12 +532,14 @@ static int enqueue_t(BatchPlan& P) {
     }
   }
   k_misfit_sum<<<1, 32, 0, st>>>(P.d_smis.as<double>(), P.ns, P.d_mis.as<double>());
-  ADT_CUDA(cudaEventRecord(P.ev[4 * P.chunks.size() + 1], st));
+  ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * P.chunks.size() + 1], st, evf));
   ADT_CUDA(cudaGetLastError());
   return ADT_OK;
 }
 
-static int enqueue(BatchPlan& P) { return P.f64 ? enqueue_t<double>(P) : enqueue_t<float>(P); }
+static int enqueue(BatchPlan& P, bool capturing) {
+  return P.f64 ? enqueue_t<double>(P, capturing) : enqueue_t<float>(P, capturing);
+}
 
 int batch_upload(BatchPlan* P, const double* slowness, const double* t_obs, const double* weight) {
   if (slowness) {
@@ -515,7 +555,7 @@ int batch_upload(BatchPlan* P, const double* slowness, const double* t_obs, cons
 
 int batch_run_resident(BatchPlan* P) {
   if (!P->opts.use_graph) {
-    int rc = enqueue(*P);
+    int rc = enqueue(*P, false);
     if (rc) return rc;
     P->ran = true;
     return ADT_OK;
@@ -523,7 +563,7 @@ int batch_run_resident(BatchPlan* P) {
   if (!P->graph) {
     cudaGraph_t g = nullptr;
     ADT_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue(*P);
+    int rc = enqueue(*P, true);
     cudaError_t e = cudaStreamEndCapture(P->stream, &g);
     if (rc) {
       if (g) cudaGraphDestroy(g);
@@ -554,7 +594,8 @@ int batch_download(BatchPlan* P, double* misfit, double* t_pred, double* grad,
 int batch_stats(BatchPlan* P, adt_batch_stats* s) {
   std::memset(s, 0, sizeof(*s));
   s->bk = P->bk;
-  s->warps = P->fwd_warps;
+  s->warps = P->fwd_gw;
+  s->groups = P->fwd_groups;
   s->ctas = P->fwd_ctas;
   s->fwd_ms = s->adj_ms = s->total_ms = -1.f;
   if (!P->ran) return ADT_OK;

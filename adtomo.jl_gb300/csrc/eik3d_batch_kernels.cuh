@@ -1,10 +1,12 @@
 // eik3d_batch_kernels.cuh -- kernels of the batched misfit + gradient plan.
 //
-// A persistent grid of CTAs; each CTA takes one solve at a time from a work
-// counter (solves pre-sorted largest grid first) and runs that solve's whole
-// forward (or adjoint) alone, so a CTA needs no other CTA: the only
-// synchronisation is __syncthreads between brick levels.  Inside a solve the
-// CTA's warps sweep the bricks of one level concurrently (eik3d_brick.cuh).
+// A persistent grid of CTAs, each split into warp groups.  A group takes one
+// solve at a time from a work counter (solves pre-sorted largest grid first)
+// and runs that solve's whole forward (or adjoint) alone, so no group ever
+// waits for another: the only synchronisation is a named barrier of the
+// group's warps between brick levels.  Inside a solve the group's warps sweep
+// the dirty bricks of one level concurrently (eik3d_brick.cuh); several
+// groups per SM keep the SM busy while one solve's level has little work.
 //
 // Brick skipping (exact): a brick is swept in an ordering only if it, or one
 // of its six face neighbours, changed since the brick was last swept.  A
@@ -13,6 +15,18 @@
 // leaves every result bit-identical to sweeping everything.
 #pragma once
 #include "eik3d_brick.cuh"
+
+// Register budget of the persistent sweep kernels: threads per CTA the
+// compiler must fit (0 = unconstrained).  65536 / ADT_BATCH_MAXT registers
+// per thread.
+#ifndef ADT_BATCH_MAXT
+#define ADT_BATCH_MAXT 0
+#endif
+#if ADT_BATCH_MAXT > 0
+#define ADT_BATCH_BOUNDS __launch_bounds__(ADT_BATCH_MAXT, 1)
+#else
+#define ADT_BATCH_BOUNDS
+#endif
 
 namespace adt {
 
@@ -63,7 +77,28 @@ struct BatchArgs {
   int adj_max_iter;
   int ref_compat;
   int near_r;
+  int group_warps;          // warps per group (one solve per group)
+  int meta_smem;            // 1: brick meta of the running solve in shared memory
+  int max_nb;               // bricks of the largest field (shared-memory meta size)
 };
+
+// Per-group scalars at the start of dynamic shared memory.
+struct GroupShared {
+  int q;
+  int changed;
+  unsigned long long err;
+};
+
+__device__ __forceinline__ void group_sync(int grp, int nthreads) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(grp + 1), "r"(nthreads) : "memory");
+}
+
+// Dynamic shared memory: [G GroupShared][G * 2 * max_nb meta ints][warp tiles]
+__host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_nb) {
+  size_t b = ((size_t)G * sizeof(GroupShared) + 15) / 16 * 16;
+  if (meta_smem) b += ((size_t)G * 2 * max_nb * sizeof(int) + 15) / 16 * 16;
+  return b;
+}
 
 // Initial value of the implicit u0 (scripts/gene_obs.jl:44-51): 1000, or the
 // FP64 distance value at the 8 nodes around the source.
@@ -122,38 +157,103 @@ __device__ __forceinline__ bool brick_needed(const int* mod, const int* proc, co
 }
 
 // ------------------------------------------------------------------ forward
+// Group layout helpers shared by the forward and adjoint kernels.
+struct GroupCtx {
+  int NW, GW, G, warp, lane, grp, gw, gthreads;
+  GroupShared* gs;
+  int* smeta;  // this group's meta (2 * max_nb ints) or null
+  unsigned char* tiles;
+};
+
+template <class T>
+__device__ __forceinline__ GroupCtx group_ctx(const BatchArgs<T>& A, unsigned char* smem) {
+  GroupCtx c;
+  c.NW = blockDim.x >> 5;
+  c.GW = A.group_warps;
+  c.G = c.NW / c.GW;
+  c.warp = threadIdx.x >> 5;
+  c.lane = threadIdx.x & 31;
+  c.grp = c.warp / c.GW;
+  c.gw = c.warp - c.grp * c.GW;
+  c.gthreads = c.GW * 32;
+  c.gs = reinterpret_cast<GroupShared*>(smem) + c.grp;
+  const size_t g0 = ((size_t)c.G * sizeof(GroupShared) + 15) / 16 * 16;
+  c.smeta = A.meta_smem ? reinterpret_cast<int*>(smem + g0) + (size_t)c.grp * 2 * A.max_nb : nullptr;
+  c.tiles = smem + group_hdr_bytes(c.G, A.meta_smem, A.max_nb);
+  return c;
+}
+
+// Take the next solve for this group (or -1 when the queue is empty).  The
+// first solve of every group is assigned round-robin across CTAs (group g of
+// CTA b takes g * gridDim.x + b), so every SM gets a solve before any SM
+// gets a second; later solves come from the shared counter.
+template <class T>
+__device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx& c, bool& first) {
+  int q;
+  if (first) {
+    first = false;
+    q = c.grp * (int)gridDim.x + (int)blockIdx.x;
+  } else {
+    if (c.gw == 0 && c.lane == 0) c.gs->q = atomicAdd(A.next, 1) + c.G * (int)gridDim.x;
+    group_sync(c.grp, c.gthreads);
+    q = c.gs->q;
+    group_sync(c.grp, c.gthreads);
+  }
+  return q < A.n_solves ? q : -1;
+}
+
+// Select the sweep instantiation for the ordering's tile stride, k direction
+// and near-source flag.
+template <int BK>
+__device__ __forceinline__ bool dispatch_fwd_f32(float* S, const float* F, const BrickPos& p,
+                                                 int si, int sj, int sk, bool nr, float h,
+                                                 double hd, const NearBox& box, int lane,
+                                                 float& md) {
+  constexpr int C9 = tile_col_stride(BK, true), C7 = tile_col_stride(BK, false);
+  const bool same = (sj == sk);
+  if (sk > 0) {
+    if (same)
+      return nr ? sweep_brick_fwd_f32<BK, C9, true, true>(S, F, p, si, sj, h, hd, box, lane, md)
+                : sweep_brick_fwd_f32<BK, C9, true, false>(S, F, p, si, sj, h, hd, box, lane, md);
+    return nr ? sweep_brick_fwd_f32<BK, C7, true, true>(S, F, p, si, sj, h, hd, box, lane, md)
+              : sweep_brick_fwd_f32<BK, C7, true, false>(S, F, p, si, sj, h, hd, box, lane, md);
+  }
+  if (same)
+    return nr ? sweep_brick_fwd_f32<BK, C9, false, true>(S, F, p, si, sj, h, hd, box, lane, md)
+              : sweep_brick_fwd_f32<BK, C9, false, false>(S, F, p, si, sj, h, hd, box, lane, md);
+  return nr ? sweep_brick_fwd_f32<BK, C7, false, true>(S, F, p, si, sj, h, hd, box, lane, md)
+            : sweep_brick_fwd_f32<BK, C7, false, false>(S, F, p, si, sj, h, hd, box, lane, md);
+}
+
 template <class T, int BK, int MODE>
-__global__ void k_batch_fwd(BatchArgs<T> A) {
+__global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int s_q;
-  __shared__ unsigned long long s_err;
-  const int NW = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* S = reinterpret_cast<T*>(smem) + warp * (tile_elems(BK) + itile_elems(BK));
+  const GroupCtx c = group_ctx(A, smem);
+  if (c.grp >= c.G) return;
+  const int lane = c.lane;
+  T* S = reinterpret_cast<T*>(c.tiles) + c.warp * (tile_elems(BK) + itile_elems(BK));
   T* F = S + tile_elems(BK);
   unsigned long long cnt_upd = 0, cnt_brk = 0;
+  bool first = true;
   for (;;) {
-    if (threadIdx.x == 0) s_q = atomicAdd(A.next, 1);
-    __syncthreads();
-    const int q = s_q;
-    __syncthreads();
-    if (q >= A.n_solves) break;
-    const int gs = A.order[q];
-    const SolveDev sd = A.solves[gs];
+    const int q = group_next(A, c, first);
+    if (q < 0) break;
+    const int gsol = A.order[q];
+    const SolveDev& sd = A.solves[gsol];
     const FieldDev<T> fd = A.fields[sd.field];
     const Geom g = fd.g;
     const T h = (T)fd.h;
     T* u = A.u + sd.u_off;
     const int nb = g.nbx * g.nby * g.nbz;
-    int* mod = A.meta + sd.meta_off;
-    int* proc = mod + nb;
+    int* mod = c.smeta ? c.smeta : A.meta + sd.meta_off;
+    int* proc = mod + (c.smeta ? A.max_nb : nb);
     // u = u0 (column-wise: lanes along k)
-    for (int64_t col = warp; col < (int64_t)g.m * g.n; col += NW) {
+    for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
       T* uc = u + col * g.l;
       for (int k = lane; k < g.l; k += 32) uc[k] = (T)u0_at(sd, i, j, k);
     }
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
       mod[b] = -1;
       proc[b] = -1;
     }
@@ -165,16 +265,17 @@ __global__ void k_batch_fwd(BatchArgs<T> A) {
     box.k0 = max(0, sd.zf - A.near_r);
     box.k1 = min(g.l - 1, sd.zc + A.near_r);
     const bool use_near = (A.near_r >= 0) && (MODE == MODE_STABLE);
-    T* snap = A.snap ? A.snap + blockIdx.x * A.snap_stride : nullptr;
-    __syncthreads();
+    const bool vec = (g.l % 4) == 0;
+    T* snap = A.snap ? A.snap + (int64_t)(blockIdx.x * c.G + c.grp) * A.snap_stride : nullptr;
+    group_sync(c.grp, c.gthreads);
     int it;
     bool conv = false;
     T err = T(0);
     for (it = 0; it < A.max_iter; ++it) {
-      if (threadIdx.x == 0) s_err = 0ull;
+      if (c.gw == 0 && lane == 0) c.gs->err = 0ull;
       if (snap)
-        for (int64_t c = threadIdx.x; c < g.ncell; c += blockDim.x) snap[c] = u[c];
-      __syncthreads();
+        for (int64_t x = c.gw * 32 + lane; x < g.ncell; x += c.gthreads) snap[x] = u[x];
+      group_sync(c.grp, c.gthreads);
       T md = T(0);
       for (int o = 0; o < 8; ++o) {
         int si, sj, sk;
@@ -183,16 +284,36 @@ __global__ void k_batch_fwd(BatchArgs<T> A) {
         for (int d = 0; d < g.nlev; ++d) {
           const int t = (it * 8 + o) * g.nlev + d;
           const int q1 = fd.lstart[d + 1];
-          for (int qq = fd.lstart[d] + warp; qq < q1; qq += NW) {
+          for (int qq = fd.lstart[d] + c.gw; qq < q1; qq += c.GW) {
             const BrickPos p = brick_pos<BK>(g, fd.bricks[qq], si, sj, sk);
             if (!brick_needed(mod, proc, g, p, lane)) continue;
-            load_halo_tile<T, BK>(S, u, g, p, CS, lane);
-            load_interior<T, BK>(F, fd.f, g, p, CS, lane);
-            cp_async_wait_all();
-            __syncwarp();
-            const bool ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
-                                                         use_near && box.hits(p), lane, md);
-            if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
+            bool ch;
+            if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
+              if (vec) {
+                load_tile_f32_vec<BK>(S, u, g, p, CS, lane);
+                load_interior_f32_vec<BK>(F, fd.f, g, p, CS, lane);
+                __syncwarp();
+                const bool nr = use_near && box.hits(p);
+                ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, md);
+                if (ch) store_interior_f32_vec<BK>(S, u, g, p, CS, lane);
+              } else {
+                load_halo_tile<T, BK>(S, u, g, p, CS, lane);
+                load_interior<T, BK>(F, fd.f, g, p, CS, lane);
+                cp_async_wait_all();
+                __syncwarp();
+                ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
+                                                  use_near && box.hits(p), lane, md);
+                if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
+              }
+            } else {
+              load_halo_tile<T, BK>(S, u, g, p, CS, lane);
+              load_interior<T, BK>(F, fd.f, g, p, CS, lane);
+              cp_async_wait_all();
+              __syncwarp();
+              ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
+                                                use_near && box.hits(p), lane, md);
+              if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
+            }
             __syncwarp();
             if (lane == 0) {
               const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
@@ -202,28 +323,28 @@ __global__ void k_batch_fwd(BatchArgs<T> A) {
               cnt_brk += 1;
             }
           }
-          __syncthreads();
+          group_sync(c.grp, c.gthreads);
         }
       }
       if (snap) {
         T mx = T(0);
-        for (int64_t c = threadIdx.x; c < g.ncell; c += blockDim.x) {
-          const T dd = u[c] > snap[c] ? u[c] - snap[c] : snap[c] - u[c];
+        for (int64_t x = c.gw * 32 + lane; x < g.ncell; x += c.gthreads) {
+          const T dd = u[x] > snap[x] ? u[x] - snap[x] : snap[x] - u[x];
           mx = rmax(dd, mx);
         }
         md = mx;
       }
       md = warp_max(md);
-      if (lane == 0) atomicMax(&s_err, to_ordered<T>(md));
-      __syncthreads();
-      err = from_ordered<T>(s_err);
-      __syncthreads();
+      if (lane == 0) atomicMax(&c.gs->err, to_ordered<T>(md));
+      group_sync(c.grp, c.gthreads);
+      err = from_ordered<T>(c.gs->err);
+      group_sync(c.grp, c.gthreads);
       if ((double)err < A.tol) {
         conv = true;
         break;
       }
     }
-    if (threadIdx.x == 0) {
+    if (c.gw == 0 && lane == 0) {
       adt_solve_status& st = A.status[sd.gidx];
       st.iters = conv ? it + 1 : it;
       st.converged = conv ? 1 : 0;
@@ -399,96 +520,107 @@ __device__ __forceinline__ int upwind_side_t(const T* u, int64_t c, int pos, int
   return (uc > a) ? side : 0;
 }
 
+template <int BK>
+__device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const uint16_t* C,
+                                                 const int64_t* sidx, const float* sval,
+                                                 int ns, const Geom& g, const BrickPos& p, int si,
+                                                 int sj, int sk, int lane) {
+  constexpr int C9 = tile_col_stride(BK, true), C7 = tile_col_stride(BK, false);
+  if (sk > 0)
+    return (sj == sk) ? sweep_brick_adj_f32<BK, C9, true>(U, L, C, sidx, sval, ns, g, p, si, sj, lane)
+                      : sweep_brick_adj_f32<BK, C7, true>(U, L, C, sidx, sval, ns, g, p, si, sj, lane);
+  return (sj == sk) ? sweep_brick_adj_f32<BK, C9, false>(U, L, C, sidx, sval, ns, g, p, si, sj, lane)
+                    : sweep_brick_adj_f32<BK, C7, false>(U, L, C, sidx, sval, ns, g, p, si, sj, lane);
+}
+
 template <class T, int BK>
-__global__ void k_batch_adj(BatchArgs<T> A) {
+__global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int s_q;
-  __shared__ int s_changed;
-  const int NW = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const GroupCtx c = group_ctx(A, smem);
+  if (c.grp >= c.G) return;
+  const int lane = c.lane;
   constexpr size_t WS = (2 * tile_elems(BK)) * sizeof(T) + itile_elems(BK) * sizeof(uint16_t);
-  T* U = reinterpret_cast<T*>(smem + warp * WS);
+  T* U = reinterpret_cast<T*>(c.tiles + c.warp * WS);
   T* L = U + tile_elems(BK);
   uint16_t* C = reinterpret_cast<uint16_t*>(L + tile_elems(BK));
   unsigned long long cnt_upd = 0, cnt_brk = 0;
   constexpr bool EXACT = sizeof(T) == 8;
+  bool first = true;
   for (;;) {
-    if (threadIdx.x == 0) s_q = atomicAdd(A.next, 1);
-    __syncthreads();
-    const int q = s_q;
-    __syncthreads();
-    if (q >= A.n_solves) break;
-    const int gs = A.order[q];
-    const SolveDev sd = A.solves[gs];
+    const int q = group_next(A, c, first);
+    if (q < 0) break;
+    const int gsol = A.order[q];
+    const SolveDev& sd = A.solves[gsol];
     const FieldDev<T> fd = A.fields[sd.field];
     const Geom g = fd.g;
     const T* u = A.u + sd.u_off;
     T* lam = A.lam + sd.u_off;
     uint16_t* code = A.code + sd.u_off;
     const int nb = g.nbx * g.nby * g.nbz;
-    int* mod = A.meta + sd.meta_off;
-    int* proc = mod + nb;
+    int* mod = c.smeta ? c.smeta : A.meta + sd.meta_off;
+    int* proc = mod + (c.smeta ? A.max_nb : nb);
     const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+    const bool vec = (g.l % 8) == 0;
     // pass 1: upwind sides and fixed cells; lambda = 0
-    for (int64_t col = warp; col < (int64_t)g.m * g.n; col += NW) {
+    for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
       for (int k = lane; k < g.l; k += 32) {
-        const int64_t c = col * g.l + k;
-        const T uc = u[c];
-        const int sx = upwind_side_t(u, c, i, g.m, sI, uc);
-        const int sy = upwind_side_t(u, c, j, g.n, sJ, uc);
-        const int sz = upwind_side_t(u, c, k, g.l, (int64_t)1, uc);
+        const int64_t x = col * g.l + k;
+        const T uc = u[x];
+        const int sx = upwind_side_t(u, x, i, g.m, sI, uc);
+        const int sy = upwind_side_t(u, x, j, g.n, sJ, uc);
+        const int sz = upwind_side_t(u, x, k, g.l, (int64_t)1, uc);
         uint16_t cd = (uint16_t)(sx | (sy << 2) | (sz << 4));
         if (uc == (T)u0_at(sd, i, j, k) || (sx | sy | sz) == 0) cd = CODE_FIXED;
-        code[c] = cd;
-        lam[c] = T(0);
+        code[x] = cd;
+        lam[x] = T(0);
       }
     }
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
       mod[b] = -2;
       proc[b] = -1;
     }
-    __syncthreads();
+    group_sync(c.grp, c.gthreads);
     // pass 2: users (reads only the low bits of neighbours, writes own high bits)
-    for (int64_t col = warp; col < (int64_t)g.m * g.n; col += NW) {
+    for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
       for (int k = lane; k < g.l; k += 32) {
-        const int64_t c = col * g.l + k;
-        const uint16_t cd = code[c];
+        const int64_t x = col * g.l + k;
+        const uint16_t cd = code[x];
         if (cd & CODE_FIXED) continue;
         uint16_t us = 0;
         auto uses = [&](int64_t r, int ax, int want) -> bool {
           const uint16_t cr = code[r];
           return !(cr & CODE_FIXED) && (((cr >> (2 * ax)) & 3) == want);
         };
-        if (i > 0 && uses(c - sI, 0, 2)) us |= 1;
-        if (i < g.m - 1 && uses(c + sI, 0, 1)) us |= 2;
-        if (j > 0 && uses(c - sJ, 1, 2)) us |= 4;
-        if (j < g.n - 1 && uses(c + sJ, 1, 1)) us |= 8;
-        if (k > 0 && uses(c - 1, 2, 2)) us |= 16;
-        if (k < g.l - 1 && uses(c + 1, 2, 1)) us |= 32;
-        code[c] = (uint16_t)(cd | (us << CODE_USERS));
+        if (i > 0 && uses(x - sI, 0, 2)) us |= 1;
+        if (i < g.m - 1 && uses(x + sI, 0, 1)) us |= 2;
+        if (j > 0 && uses(x - sJ, 1, 2)) us |= 4;
+        if (j < g.n - 1 && uses(x + sJ, 1, 1)) us |= 8;
+        if (k > 0 && uses(x - 1, 2, 2)) us |= 16;
+        if (k < g.l - 1 && uses(x + 1, 2, 1)) us |= 32;
+        code[x] = (uint16_t)(cd | (us << CODE_USERS));
       }
     }
-    __syncthreads();
+    group_sync(c.grp, c.gthreads);
     // seeds: mark cells and make their bricks dirty
     const int ns = A.n_seed[sd.gidx];
     const int64_t* sidx = A.seed_idx + sd.seed_off;
     const T* sval = A.seed_val + sd.seed_off;
-    for (int e = threadIdx.x; e < ns; e += blockDim.x) {
-      const int64_t c = sidx[e];
-      const uint16_t cd = code[c];
+    for (int e = c.gw * 32 + lane; e < ns; e += c.gthreads) {
+      const int64_t x = sidx[e];
+      const uint16_t cd = code[x];
       if (cd & CODE_FIXED) continue;
-      code[c] = (uint16_t)(cd | CODE_SEED);
-      const int i = (int)(c / sI), j = (int)((c / sJ) % g.n), k = (int)(c % g.l);
+      code[x] = (uint16_t)(cd | CODE_SEED);
+      const int i = (int)(x / sI), j = (int)((x / sJ) % g.n), k = (int)(x % g.l);
       mod[((i / BI) * g.nby + (j / BJ)) * g.nbz + (k / BK)] = -1;
     }
-    __syncthreads();
+    group_sync(c.grp, c.gthreads);
     int it;
     bool conv = false;
     for (it = 0; it < A.adj_max_iter; ++it) {
-      if (threadIdx.x == 0) s_changed = 0;
-      __syncthreads();
+      if (c.gw == 0 && lane == 0) c.gs->changed = 0;
+      group_sync(c.grp, c.gthreads);
       bool any = false;
       for (int o = 0; o < 8; ++o) {
         int si, sj, sk;
@@ -497,17 +629,38 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         for (int d = 0; d < g.nlev; ++d) {
           const int t = (it * 8 + o) * g.nlev + d;
           const int q1 = fd.lstart[d + 1];
-          for (int qq = fd.lstart[d] + warp; qq < q1; qq += NW) {
+          for (int qq = fd.lstart[d] + c.gw; qq < q1; qq += c.GW) {
             const BrickPos p = brick_pos<BK>(g, fd.bricks[qq], si, sj, sk);
             if (!brick_needed(mod, proc, g, p, lane)) continue;
-            load_halo_tile<T, BK>(U, u, g, p, CS, lane);
-            load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
-            load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
-            cp_async_wait_all();
-            __syncwarp();
-            const bool ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g,
-                                                                 p, si, sj, sk, CS, lane);
-            if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+            bool ch;
+            if constexpr (sizeof(T) == 4) {
+              if (vec) {
+                load_tile_f32_vec<BK>(U, u, g, p, CS, lane);
+                load_tile_f32_vec<BK>(L, lam, g, p, CS, lane);
+                load_codes_vec<BK>(C, code, g, p, CS, lane);
+                __syncwarp();
+                ch = dispatch_adj_f32<BK>(U, L, C, sidx, sval, ns, g, p, si, sj, sk, lane);
+                if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
+              } else {
+                load_halo_tile<T, BK>(U, u, g, p, CS, lane);
+                load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
+                load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
+                cp_async_wait_all();
+                __syncwarp();
+                ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si,
+                                                          sj, sk, CS, lane);
+                if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+              }
+            } else {
+              load_halo_tile<T, BK>(U, u, g, p, CS, lane);
+              load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
+              load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
+              cp_async_wait_all();
+              __syncwarp();
+              ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si,
+                                                        sj, sk, CS, lane);
+              if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+            }
             __syncwarp();
             if (lane == 0) {
               const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
@@ -518,19 +671,19 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
             }
             any |= ch;
           }
-          __syncthreads();
+          group_sync(c.grp, c.gthreads);
         }
       }
-      if (any && lane == 0) s_changed = 1;
-      __syncthreads();
-      const bool changed = s_changed != 0;
-      __syncthreads();
+      if (any && lane == 0) c.gs->changed = 1;
+      group_sync(c.grp, c.gthreads);
+      const bool changed = c.gs->changed != 0;
+      group_sync(c.grp, c.gthreads);
       if (!changed) {
         conv = true;
         break;
       }
     }
-    if (threadIdx.x == 0) {
+    if (c.gw == 0 && lane == 0) {
       adt_solve_status& st = A.status[sd.gidx];
       st.adj_iters = conv ? it + 1 : it;
       st.adj_converged = conv ? 1 : 0;

@@ -199,6 +199,365 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
   return __any_sync(0xffffffffu, changed);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 staging with 16-byte vector loads (grids whose k extent is a multiple
+// of 4, so every brick column segment starts on a 16-byte boundary).  The 56
+// columns of a halo tile (32 interior, 24 face columns) are split into
+// 4-float chunks; lane t takes chunks t, t+32, ...  Out-of-grid cells of the
+// halo are written as +inf, so min(neighbour pair) falls back to the single
+// interior neighbour exactly as the reference's edge rule does.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void halo_col(int c, int& ci, int& cj) {
+  if (c < BI * BJ) {  // interior
+    ci = (c >> 2) + 1;
+    cj = (c & 3) + 1;
+  } else {
+    const int h = c - BI * BJ;  // 0..23
+    if (h < 8) {                // x faces
+      ci = (h < 4) ? 0 : BI + 1;
+      cj = (h & 3) + 1;
+    } else {                    // y faces
+      ci = ((h - 8) & 7) + 1;
+      cj = (h < 16) ? 0 : BJ + 1;
+    }
+  }
+}
+
+// Global loads of a batch are all issued before any shared store, so a
+// brick pays the memory latency once per batch instead of once per chunk.
+constexpr int LOAD_BATCH = 7;
+
+template <int BK>
+__device__ __forceinline__ void load_tile_f32_vec(float* S, const float* __restrict__ src,
+                                                  const Geom& g, const BrickPos& p, int CS,
+                                                  int lane) {
+  constexpr int RS = tile_row_stride(BK);
+  constexpr int CH = BK / 4;
+  constexpr int NCOL = BI * BJ + 2 * BI + 2 * BJ;  // 56
+  constexpr int PER = NCOL * CH / 32;              // chunks per lane (exact)
+  static_assert(NCOL * CH % 32 == 0 && PER % LOAD_BATCH == 0, "tile chunking");
+  const float INF = __int_as_float(0x7f800000);
+  // k halo of the interior columns (lane c takes interior column c), issued first
+  const int hci = (lane >> 2) + 1, hcj = (lane & 3) + 1;
+  float hlo = INF, hhi = INF;
+  {
+    const int i = p.i0 + hci - 1, j = p.j0 + hcj - 1;
+    if (i < g.m && j < g.n) {
+      const float* col = src + ((int64_t)i * g.n + j) * g.l + p.k0;
+      if (p.k0 > 0) hlo = __ldg(col - 1);
+      if (p.k0 + p.nk < g.l) hhi = __ldg(col + p.nk);
+    }
+  }
+#pragma unroll
+  for (int b0 = 0; b0 < PER; b0 += LOAD_BATCH) {
+    float4 v[LOAD_BATCH];
+    int dst[LOAD_BATCH];
+#pragma unroll
+    for (int t = 0; t < LOAD_BATCH; ++t) {
+      const int e = lane + 32 * (b0 + t);
+      const int c = e / CH, ch = e - (e / CH) * CH;
+      int ci, cj;
+      halo_col(c, ci, cj);
+      const int i = p.i0 + ci - 1, j = p.j0 + cj - 1, k = 4 * ch;
+      v[t] = make_float4(INF, INF, INF, INF);
+      if (i >= 0 && i < g.m && j >= 0 && j < g.n && k < p.nk)
+        v[t] = __ldg(reinterpret_cast<const float4*>(src + ((int64_t)i * g.n + j) * g.l + p.k0 + k));
+      dst[t] = ci * RS + cj * CS + 1 + k;
+    }
+#pragma unroll
+    for (int t = 0; t < LOAD_BATCH; ++t) {
+      float* d = S + dst[t];
+      d[0] = v[t].x;
+      d[1] = v[t].y;
+      d[2] = v[t].z;
+      d[3] = v[t].w;
+    }
+  }
+  float* d = S + hci * RS + hcj * CS;
+  d[0] = hlo;
+  d[1 + p.nk] = hhi;
+}
+
+template <int BK>
+__device__ __forceinline__ void load_interior_f32_vec(float* S, const float* __restrict__ src,
+                                                      const Geom& g, const BrickPos& p, int CS,
+                                                      int lane) {
+  constexpr int IRS = itile_row_stride(BK);
+  constexpr int CH = BK / 4;
+  constexpr int PER = BI * BJ * CH / 32;
+  constexpr int NB = PER < 8 ? PER : 8;
+  static_assert(PER % NB == 0, "interior chunking");
+#pragma unroll
+  for (int b0 = 0; b0 < PER; b0 += NB) {
+    float4 v[NB];
+    int dst[NB];
+    bool ok[NB];
+#pragma unroll
+    for (int t = 0; t < NB; ++t) {
+      const int e = lane + 32 * (b0 + t);
+      const int c = e / CH, ch = e - (e / CH) * CH;
+      const int ci = c >> 2, cj = c & 3, k = 4 * ch;
+      ok[t] = ci < p.ni && cj < p.nj && k < p.nk;
+      if (ok[t])
+        v[t] = __ldg(reinterpret_cast<const float4*>(
+            src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k));
+      dst[t] = ci * IRS + cj * CS + k;
+    }
+#pragma unroll
+    for (int t = 0; t < NB; ++t)
+      if (ok[t]) {
+        float* d = S + dst[t];
+        d[0] = v[t].x;
+        d[1] = v[t].y;
+        d[2] = v[t].z;
+        d[3] = v[t].w;
+      }
+  }
+}
+
+template <int BK>
+__device__ __forceinline__ void store_interior_f32_vec(const float* S, float* __restrict__ dst,
+                                                       const Geom& g, const BrickPos& p, int CS,
+                                                       int lane) {
+  constexpr int RS = tile_row_stride(BK);
+  constexpr int CH = BK / 4;
+  constexpr int PER = BI * BJ * CH / 32;
+#pragma unroll
+  for (int t = 0; t < PER; ++t) {
+    const int e = lane + 32 * t;
+    const int c = e / CH, ch = e - (e / CH) * CH;
+    const int ci = c >> 2, cj = c & 3, k = 4 * ch;
+    if (ci < p.ni && cj < p.nj && k < p.nk) {
+      const float* s = S + (ci + 1) * RS + (cj + 1) * CS + 1 + k;
+      *reinterpret_cast<float4*>(dst + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 +
+                                 k) = make_float4(s[0], s[1], s[2], s[3]);
+    }
+  }
+}
+
+// Hardware square root (MUFU, ~1 ulp), for the FP32 path only.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Branch-free FP32 form of upd3_stable: all three candidate roots are
+// formed and the first admissible one selected, so lanes on different
+// branches do not serialise.
+__device__ __forceinline__ float upd3_f32(float ax, float ay, float az, float fh) {
+  const float lo = fminf(fminf(ax, ay), az);
+  const float hi = fmaxf(fmaxf(ax, ay), az);
+  const float mid = fmaxf(fminf(ax, ay), fminf(fmaxf(ax, ay), az));
+  const float F2 = fh * fh;
+  const float d2 = mid - lo;
+  const float d3 = hi - lo;
+  const float e = d3 - d2;
+  const float x1 = lo + fh;
+  const float r2 = sqrt_approx(fmaxf(fmaf(-d2, d2, 2.0f * F2), 0.0f));
+  const float x2 = fmaf(0.5f, d2 + r2, lo);
+  const float r3 = sqrt_approx(fmaxf(3.0f * F2 - d2 * d2 - d3 * d3 - e * e, 0.0f));
+  const float x3 = fmaf(d2 + d3 + r3, 1.0f / 3.0f, lo);
+  return (x1 <= mid) ? x1 : ((x2 <= hi) ? x2 : x3);
+}
+
+// Shared-memory accesses with a 32-bit shared-window address and a
+// compile-time byte offset (one instruction each, no address arithmetic).
+template <int OFF>
+__device__ __forceinline__ float lds(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1+%2];\n" : "=f"(v) : "r"(a), "n"(OFF));
+  return v;
+}
+__device__ __forceinline__ void sts_if(bool p, uint32_t a, float v) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %0, 0;\n @q st.shared.f32 [%1], %2;\n}\n" ::"r"((int)p),
+      "r"(a), "f"(v)
+      : "memory");
+}
+
+// FP32 forward sweep of one staged brick (the batched path), for tiles
+// staged by load_tile_f32_vec (out-of-grid ghosts are +inf, so every
+// neighbour pair is a plain min).  Same data flow as sweep_brick_fwd; the k
+// neighbours are carried in registers: the upstream one is this lane's
+// previous result and the downstream one is loaded one step ahead and reused
+// as the next step's old value.  The step body is branch-free: lanes outside
+// their active window read a valid cell of their own column and only the
+// store and the carried state are predicated.  CS: column stride of the
+// ordering's tile layout; SKP: sweep runs towards +k.  NEAR: cells in the
+// source box update in FP64.
+template <int BK, int CS, bool SKP, bool NEAR>
+__device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, const BrickPos& p,
+                                                    int si, int sj, float h, double hd,
+                                                    const NearBox& nb, int lane, float& maxdec) {
+  constexpr int RS = tile_row_stride(BK);
+  constexpr int IRS = itile_row_stride(BK);
+  constexpr int SK = SKP ? 1 : -1;
+  const int li = lane >> 2, lj = lane & 3;
+  const int pi = si > 0 ? li : BI - 1 - li;
+  const int pj = sj > 0 ? lj : BJ - 1 - lj;
+  const int s = li + lj;
+  const bool colok = (pi < p.ni) && (pj < p.nj);
+  const int nk = colok ? p.nk : 0;
+  const int kb = SKP ? 0 : p.nk - 1;
+  const uint32_t a0 = smem_u32(S + (pi + 1) * RS + (pj + 1) * CS + 1 + kb);
+  const uint32_t fa0 = smem_u32(F + pi * IRS + pj * CS + kb);
+  float uo = lds<0>(a0);
+  float prev = lds<-4 * SK>(a0);
+  float mb = 0.0f;
+  const int nsteps = p.nk + SKEW;
+#pragma unroll 2
+  for (int tau = 0; tau < nsteps; ++tau) {
+    const int kk = tau - s;
+    const bool act = (unsigned)kk < (unsigned)nk;
+    const int kc = act ? kk : 0;
+    const uint32_t a = a0 + (uint32_t)(4 * SK * kc);
+    const float dn = lds<4 * SK>(a);
+    const float xm = lds<-4 * RS>(a), xp = lds<4 * RS>(a);
+    const float ym = lds<-4 * CS>(a), yp = lds<4 * CS>(a);
+    const float fc = lds<0>(fa0 + (uint32_t)(4 * SK * kc));
+    const float az = fminf(prev, dn);
+    const float ax = fminf(xm, xp);
+    const float ay = fminf(ym, yp);
+    float un;
+    if (NEAR && act && nb.has(p.i0 + pi, p.j0 + pj, p.k0 + kb + SK * kc))
+      un = (float)upd3_stable<double>((double)ax, (double)ay, (double)az, (double)fc * hd);
+    else
+      un = upd3_f32(ax, ay, az, fc * h);
+    const float d = act ? uo - un : 0.0f;
+    sts_if(d > 0.0f, a, un);
+    mb = fmaxf(mb, d);
+    prev = act ? fminf(un, uo) : prev;
+    uo = act ? dn : uo;
+    __syncwarp();
+  }
+  maxdec = fmaxf(maxdec, mb);
+  return __any_sync(0xffffffffu, mb > 0.0f);
+}
+
+// Interior codes (uint16) with 16-byte vector loads: 8 codes per chunk.
+// Needs the k extent to be a multiple of 8 (16-byte aligned column segments).
+template <int BK>
+__device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* __restrict__ src,
+                                               const Geom& g, const BrickPos& p, int CS, int lane) {
+  constexpr int IRS = itile_row_stride(BK);
+  constexpr int CH = BK / 8;
+  constexpr int PER = BI * BJ * CH / 32;
+  uint4 v[PER];
+  int dst[PER];
+  bool ok[PER];
+#pragma unroll
+  for (int t = 0; t < PER; ++t) {
+    const int e = lane + 32 * t;
+    const int c = e / CH, ch = e - (e / CH) * CH;
+    const int ci = c >> 2, cj = c & 3, k = 8 * ch;
+    ok[t] = ci < p.ni && cj < p.nj && k < p.nk;
+    if (ok[t])
+      v[t] = __ldg(reinterpret_cast<const uint4*>(
+          src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k));
+    dst[t] = ci * IRS + cj * CS + k;
+  }
+#pragma unroll
+  for (int t = 0; t < PER; ++t)
+    if (ok[t]) {
+      uint16_t* d = S + dst[t];
+      d[0] = (uint16_t)(v[t].x & 0xffffu);
+      d[1] = (uint16_t)(v[t].x >> 16);
+      d[2] = (uint16_t)(v[t].y & 0xffffu);
+      d[3] = (uint16_t)(v[t].y >> 16);
+      d[4] = (uint16_t)(v[t].z & 0xffffu);
+      d[5] = (uint16_t)(v[t].z >> 16);
+      d[6] = (uint16_t)(v[t].w & 0xffffu);
+      d[7] = (uint16_t)(v[t].w >> 16);
+    }
+}
+
+__device__ __forceinline__ uint32_t ldsu16(uint32_t a) {
+  unsigned short v;
+  asm volatile("ld.shared.u16 %0, [%1];\n" : "=h"(v) : "r"(a));
+  return (uint32_t)v;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// FP32 adjoint sweep of one staged brick (tiles from the vector loaders).
+// lambda_c = (g_c + 2 sum_users (u_r - u_c) lambda_r) / (2 sum_active (u_c - u_upwind)).
+// Branch-free: the six neighbours' u and lambda are loaded once and serve
+// both the user terms and the diagonal; inactive terms are selected away
+// (selects, not products, so +inf ghosts never turn into NaN).  U and L
+// share one tile layout at byte distance LOFF.  CS: column stride of the
+// ordering's layout; SKP: sweep runs towards +k.
+template <int BK, int CS, bool SKP>
+__device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, const uint16_t* C,
+                                                    const int64_t* seed_idx, const float* seed_val,
+                                                    int n_seed, const Geom& g, const BrickPos& p,
+                                                    int si, int sj, int lane) {
+  constexpr int RS = tile_row_stride(BK);
+  constexpr int IRS = itile_row_stride(BK);
+  constexpr int SK = SKP ? 1 : -1;
+  const int li = lane >> 2, lj = lane & 3;
+  const int pi = si > 0 ? li : BI - 1 - li;
+  const int pj = sj > 0 ? lj : BJ - 1 - lj;
+  const int s = li + lj;
+  const bool colok = (pi < p.ni) && (pj < p.nj);
+  const int nk = colok ? p.nk : 0;
+  const int kb = SKP ? 0 : p.nk - 1;
+  const int own = (pi + 1) * RS + (pj + 1) * CS + 1 + kb;
+  const uint32_t ua0 = smem_u32(U + own);
+  const uint32_t la0 = smem_u32(L + own);
+  const uint32_t ca0 = smem_u32(C + pi * IRS + pj * CS + kb);
+  const int64_t gcol = ((int64_t)(p.i0 + pi) * g.n + (p.j0 + pj)) * g.l + p.k0 + kb;
+  bool changed = false;
+  const int nsteps = p.nk + SKEW;
+#pragma unroll 1
+  for (int tau = 0; tau < nsteps; ++tau) {
+    const int kk = tau - s;
+    const bool act = (unsigned)kk < (unsigned)nk;
+    const int kc = act ? kk : 0;
+    const uint32_t ua = ua0 + (uint32_t)(4 * SK * kc);
+    const uint32_t la = la0 + (uint32_t)(4 * SK * kc);
+    const uint32_t code = ldsu16(ca0 + (uint32_t)(2 * SK * kc));
+    const float uc = lds<0>(ua);
+    const float u_xm = lds<-4 * RS>(ua), u_xp = lds<4 * RS>(ua);
+    const float u_ym = lds<-4 * CS>(ua), u_yp = lds<4 * CS>(ua);
+    const float u_zm = lds<-4>(ua), u_zp = lds<4>(ua);
+    const float l_xm = lds<-4 * RS>(la), l_xp = lds<4 * RS>(la);
+    const float l_ym = lds<-4 * CS>(la), l_yp = lds<4 * CS>(la);
+    const float l_zm = lds<-4>(la), l_zp = lds<4>(la);
+    const float lold = lds<0>(la);
+    const uint32_t us = code >> CODE_USERS;
+    float acc = (us & 1u) ? (u_xm - uc) * l_xm : 0.0f;
+    acc += (us & 2u) ? (u_xp - uc) * l_xp : 0.0f;
+    acc += (us & 4u) ? (u_ym - uc) * l_ym : 0.0f;
+    acc += (us & 8u) ? (u_yp - uc) * l_yp : 0.0f;
+    acc += (us & 16u) ? (u_zm - uc) * l_zm : 0.0f;
+    acc += (us & 32u) ? (u_zp - uc) * l_zp : 0.0f;
+    const uint32_t sx = code & 3u, sy = (code >> 2) & 3u, sz = (code >> 4) & 3u;
+    float d = sx ? uc - (sx == 1u ? u_xm : u_xp) : 0.0f;
+    d += sy ? uc - (sy == 1u ? u_ym : u_yp) : 0.0f;
+    d += sz ? uc - (sz == 1u ? u_zm : u_zp) : 0.0f;
+    float gs = 0.0f;
+    if (act && (code & CODE_SEED)) {
+      const int64_t key = gcol + SK * kc;
+      int lo = 0, hi = n_seed - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (seed_idx[mid] < key) lo = mid + 1; else hi = mid;
+      }
+      gs = seed_val[lo];
+    }
+    const float lam = fmaf(2.0f, acc, gs) * rcp_approx(2.0f * d);
+    const bool wr = act && !(code & CODE_FIXED) && (lam != lold);
+    sts_if(wr, la, lam);
+    changed |= wr;
+    __syncwarp();
+  }
+  return __any_sync(0xffffffffu, changed);
+}
+
 // Adjoint sweep of one staged brick: lambda_c = (g_c + sum_users 2 (u_r - u_c)
 // lambda_r) / d_c with d_c = sum_active 2 (u_c - u_upwind), fixed cells keep
 // lambda = 0 (Eikonal3D.cpp:113-196 solved by reverse sweeps; Eikonal.h:95-200

@@ -129,6 +129,27 @@ def cpu_events_per_s(sample_events, threads):
     return k / dt, dt
 
 
+def plain_fp64_events_per_s(k):
+    """The plain FP64 single-event GPU path on the same workload: one event
+    per call (adt_eikonal_three_d, then adt_eikonal_three_d_grad), no
+    batching, no graph; misfit sampling and seeds on the host."""
+    import adtomo_gb300 as A
+    from oracle import oracle as O
+    f, f_obs, sta, src, w = workload()
+    t_obs = np.full(N_STA, 1.0)
+    t0 = time.perf_counter()
+    for e in range(k):
+        u0 = O.src_u0(f, H, src[e])
+        u = A.eikonal3d(u0, f, H, M, N, L, 1e-6)
+        gu = np.zeros_like(u)
+        for q in range(N_STA):
+            t, idx, wt = O.sample(u, sta[q])
+            np.add.at(gu.ravel(), idx, -2.0 * (t_obs[q] - t) * wt)
+        A.eikonal3d_grad(gu, u, u0, f, H, M, N, L)
+    dt = time.perf_counter() - t0
+    return k / dt, dt
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -166,7 +187,8 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     f, f_obs, sta, src, w = workload()
     sf = np.zeros(N_EVENTS, np.int32)
-    B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6)
+    B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
+                  warps=args.warps, groups=args.groups)
     # observed times from the +2% noise model (setup, untimed)
     B.upload([f_obs], np.full(N_EVENTS * N_STA, 1.0), w)
     B.run_resident()
@@ -230,6 +252,8 @@ def run_ours(args, rank, world):
     cpu_sample = max(threads, 16) if args.cpu_sample is None else args.cpu_sample
     cpu_val, cpu_dt = (cpu_events_per_s(cpu_sample, threads) if cpu_sample > 0 else (None, 0.0))
     iters = [s.iters for s in status]
+    plain_val, plain_dt = (plain_fp64_events_per_s(args.plain_sample) if args.plain_sample > 0
+                           else (None, 0.0))
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -240,7 +264,8 @@ def run_ours(args, rank, world):
                                "summed slowness gradient",
                    "events_per_gpu": N_EVENTS, "grid": [M, N, L], "l2": "inputs larger than L2 "
                    "(1 GB of travel times + 1 GB of adjoint variables per step)",
-                   "bk": st.bk, "warps_per_cta": st.warps, "ctas": st.ctas,
+                   "bk": st.bk, "warps_per_solve": st.warps, "solves_per_cta": st.groups,
+                   "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status]))},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
@@ -258,6 +283,10 @@ def run_ours(args, rank, world):
                           "sample": f"{cpu_sample} of the 256 events (oracle port of "
                                     f"Eikonal3D.cpp, FP64, tol 1e-6, 20-iteration cap), "
                                     f"{cpu_dt:.1f} s"} if cpu_val else None),
+        "plain_fp64": ({"value": plain_val, "unit": "events/s",
+                        "sample": f"{args.plain_sample} events, one per call through "
+                                  f"adt_eikonal_three_d + adt_eikonal_three_d_grad (FP64, "
+                                  f"host buffers), {plain_dt:.2f} s"} if plain_val else None),
         "clocks": clocks,
         "gpu_launches": 7 * args.steps,
     }
@@ -274,6 +303,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--events", type=int, default=N_EVENTS,
                     help="events per GPU (default 256, the workload; smaller for profiling)")
+    ap.add_argument("--bk", type=int, default=0, help="brick depth (0 = library default)")
+    ap.add_argument("--warps", type=int, default=0, help="warps per solve (0 = default)")
+    ap.add_argument("--groups", type=int, default=0, help="solves per CTA (0 = as many as fit)")
+    ap.add_argument("--plain-sample", type=int, default=4,
+                    help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,
                     help="events timed for the cpu_baseline (0 skips it)")
     args = ap.parse_args()
