@@ -42,7 +42,7 @@ M, N, L, H = 128, 128, 64, 0.5
 N_EVENTS, N_STA = 256, 100
 SEED = 0
 BYTES_PER_FWD_UPDATE = 12  # FP32: read u, read f, write u per cell-update
-BYTES_PER_ADJ_UPDATE = 16  # FP32: read u, read/write lambda, code (2 B) rounded
+BYTES_PER_ADJ_UPDATE = 14  # FP32: read u, read code (2 B), read and write lambda
 
 
 def workload():
@@ -237,17 +237,29 @@ def run_ours(args, rank, world):
     value = N_EVENTS * world / (ms_step / 1000.0)
     e2e_val = N_EVENTS * world / (e2e_ms / 1000.0 / args.steps)
     peak, peak_kind = peaks()
-    achieved = upd_f[-1] * BYTES_PER_FWD_UPDATE / (fwd_ms[-1] / 1000.0) / 1e9
+    traffic = {}
+    prof = os.path.join(ROOT, "profiles", "k_batch_sweeps_c3_dram_traffic.json")
+    if os.path.exists(prof) and N_EVENTS == 256:
+        try:
+            d = json.load(open(prof))
+            traffic = {k: d[k]["traffic_bytes_per_launch"] for k in ("k_batch_fwd", "k_batch_adj")}
+        except (OSError, ValueError, KeyError):
+            traffic = {}
+    kern = {
+        "k_batch_fwd": {"launch_ms": fwd_ms[-1], "cell_updates": int(upd_f[-1]),
+                        "bytes_per_update": BYTES_PER_FWD_UPDATE},
+        "k_batch_adj": {"launch_ms": adj_ms[-1], "cell_updates": int(upd_a[-1]),
+                        "bytes_per_update": BYTES_PER_ADJ_UPDATE},
+    }
+    for k, v in kern.items():
+        v["achieved_GBs"] = v["cell_updates"] * v["bytes_per_update"] / (v["launch_ms"] / 1e3) / 1e9
+        v["traffic"] = traffic.get(k)
+    dom = max(kern, key=lambda k: kern[k]["launch_ms"])
+    other = [k for k in kern if k != dom][0]
+    achieved = kern[dom]["achieved_GBs"]
     n_obs = N_EVENTS * N_STA
     h2d = M * N * L * 8 + 2 * n_obs * 8
     d2h = 8 + n_obs * 8 + M * N * L * 8 + N_EVENTS * 24
-    ncu_traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_batch_fwd_c3_traffic.json")
-    if os.path.exists(prof):
-        try:
-            ncu_traffic = json.load(open(prof)).get("traffic_bytes_per_launch")
-        except (OSError, ValueError):
-            ncu_traffic = None
     threads = os.cpu_count() or 1
     cpu_sample = max(threads, 16) if args.cpu_sample is None else args.cpu_sample
     cpu_val, cpu_dt = (cpu_events_per_s(cpu_sample, threads) if cpu_sample > 0 else (None, 0.0))
@@ -271,13 +283,11 @@ def run_ours(args, rank, world):
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": ncu_traffic,
-                     "kernel": "k_batch_fwd (forward sweeps)", "peak_source": peak_kind,
-                     "bytes_per_update": BYTES_PER_FWD_UPDATE,
-                     "cell_updates_per_launch": int(upd_f[-1]), "launch_ms": fwd_ms[-1],
-                     "adjoint": {"launch_ms": adj_ms[-1], "cell_updates": int(upd_a[-1]),
-                                 "achieved_GBs": upd_a[-1] * BYTES_PER_ADJ_UPDATE /
-                                 (adj_ms[-1] / 1000.0) / 1e9}},
+                     "frac": achieved / peak, "traffic": kern[dom]["traffic"], "kernel": dom,
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "bytes_per_update": kern[dom]["bytes_per_update"],
+                     "cell_updates_per_launch": kern[dom]["cell_updates"],
+                     "launch_ms": kern[dom]["launch_ms"], other: kern[other]},
         "cell_updates_per_s": (upd_f[-1] + upd_a[-1]) / (ms_step / 1000.0),
         "cpu_baseline": ({"value": cpu_val, "unit": "events/s", "cores": threads, "kind": "port",
                           "sample": f"{cpu_sample} of the 256 events (oracle port of "
