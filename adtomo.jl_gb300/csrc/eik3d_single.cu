@@ -16,15 +16,9 @@
 #include "eik3d_brick.cuh"
 #include "eik3d_common_host.h"
 #include "eik3d_single.h"
+#include "eik3d_single_kernels.h"
 
 namespace adt {
-
-constexpr int SBK = 32;        // brick depth of the single-solve path
-constexpr int FWD_WPB = 4;     // warps (bricks) per CTA, forward
-constexpr int ADJ_WPB = 2;     // warps per CTA, adjoint
-constexpr size_t FWD_WARP_SMEM = (tile_elems(SBK) + itile_elems(SBK)) * sizeof(double);
-constexpr size_t ADJ_WARP_SMEM =
-    (2 * tile_elems(SBK) + itile_elems(SBK)) * sizeof(double) + itile_elems(SBK) * sizeof(uint16_t);
 
 __global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f, Geom g,
                             const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h) {

@@ -1,0 +1,22 @@
+// eik3d_single_kernels.h -- kernels and launch constants of the plain FP64
+// single-solve 3D path (defined in eik3d_single.cu).
+#pragma once
+#include "eik3d_brick.cuh"
+
+namespace adt {
+
+constexpr int SBK = 32;        // brick depth of the single-solve path
+constexpr int FWD_WPB = 4;     // warps (bricks) per CTA, forward
+constexpr int ADJ_WPB = 2;     // warps per CTA, adjoint
+constexpr size_t FWD_WARP_SMEM = (tile_elems(SBK) + itile_elems(SBK)) * sizeof(double);
+constexpr size_t ADJ_WARP_SMEM =
+    (2 * tile_elems(SBK) + itile_elems(SBK)) * sizeof(double) + itile_elems(SBK) * sizeof(uint16_t);
+
+// One level of one ordering: one warp per brick of the level.
+__global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f, Geom g,
+                            const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h);
+// max |a - b| as the bit pattern of a non-negative double (atomicMax into *out).
+__global__ void k_maxdiff(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+                          unsigned long long* out);
+
+}  // namespace adt

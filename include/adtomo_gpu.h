@@ -109,6 +109,24 @@ int adt_eikonal_three_d_grad_device(const double* grad_u, const double* u, const
                                     const double* f, double h, int64_t m, int64_t n, int64_t l,
                                     double* grad_u0, double* grad_f, void* stream);
 
+/* The 3D op on DEVICE pointers without any device allocation.  No
+ * counterpart in the reference: for callers that cannot call cudaMalloc
+ * (a framework owning the device heap through its own allocator, hosts with
+ * a memory budget fixed at start-up, callers that must not see an allocation
+ * fail mid-run).  Same kernels and results as adt_eikonal_three_d_device; the
+ * scratch (previous iterate, brick list, error word) is a fixed array of
+ * ADT_NOALLOC_SCRATCH_BYTES in the library, resident on every device that
+ * loads it until exit.  Grids above ADT_NOALLOC_MAX_CELLS cells return
+ * ADT_EINVAL.  The first call on a device looks up the array's address and
+ * should come before any stream capture on that device.  All calls on a
+ * device share the array: they must not overlap on the GPU (host threads
+ * are serialised by the library; the call returns when its work is done). */
+#define ADT_NOALLOC_MAX_CELLS 262144
+#define ADT_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024 + 128 * 1024 + 256)
+int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double h, int64_t m,
+                                       int64_t n, int64_t l, double tol, int verbose, double* u,
+                                       adt_solve_status* status, void* stream);
+
 /* ------------------------------------------------------------------------
  * Batched misfit + slowness gradient: the per-evaluation loop of
  * scripts/inversion.jl:46-105 (per-source eikonal3d, trilinear sampling at
