@@ -36,11 +36,12 @@ constexpr int BJ = 4;
 // column (pi, pj) for pi in [-1, BI], pj in [-1, BJ]; slot k+1 for k in
 // [-1, BK].  addr = (pi+1)*row + (pj+1)*col + (k+1).
 // The wavefront of one step touches cells on a local hyperplane; with
-// row = 0 (mod 32) and col = 9 (mod 32) when the j and k sweep directions
-// agree (7 otherwise), the 32 cells of every step and of each of their six
-// neighbour sets fall in 32 distinct banks for all 8 orderings.
+// row = 0 (mod 32) and col = 9 (mod 16) when the j and k sweep directions
+// agree (7 (mod 16) otherwise), the 32 cells of every step and of each of
+// their six neighbour sets fall in 32 distinct banks for all 8 orderings
+// (checked exhaustively for BK = 16, 32, 64).
 __host__ __device__ constexpr int tile_col_stride(int BK, bool same_dir) {
-  return ((BK + 2 + 31 - (same_dir ? 9 : 7)) / 32) * 32 + (same_dir ? 9 : 7);
+  return ((BK + 2 + 15 - (same_dir ? 9 : 7)) / 16) * 16 + (same_dir ? 9 : 7);
 }
 __host__ __device__ constexpr int tile_col_stride_max(int BK) {
   return tile_col_stride(BK, true) > tile_col_stride(BK, false) ? tile_col_stride(BK, true)

@@ -61,13 +61,15 @@ int grid1d(int64_t n) {
 
 template <class T>
 size_t fwd_warp_smem(int bk) {
-  return (bk == 64 ? (tile_elems(64) + itile_elems(64)) : (tile_elems(32) + itile_elems(32))) *
-         sizeof(T);
+  const int t = bk == 64 ? tile_elems(64) + itile_elems(64)
+                         : bk == 16 ? tile_elems(16) + itile_elems(16) : tile_elems(32) + itile_elems(32);
+  return (size_t)t * sizeof(T);
 }
 template <class T>
 size_t adj_warp_smem(int bk) {
-  return bk == 64 ? 2 * tile_elems(64) * sizeof(T) + itile_elems(64) * sizeof(uint16_t)
-                  : 2 * tile_elems(32) * sizeof(T) + itile_elems(32) * sizeof(uint16_t);
+  const int te = bk == 64 ? tile_elems(64) : bk == 16 ? tile_elems(16) : tile_elems(32);
+  const int ie = bk == 64 ? itile_elems(64) : bk == 16 ? itile_elems(16) : itile_elems(32);
+  return 2 * (size_t)te * sizeof(T) + (size_t)ie * sizeof(uint16_t);
 }
 
 }  // namespace
@@ -87,6 +89,9 @@ static KernelSet kernels_for(int bk) {
   if (bk == 64) {
     k.fwd = (const void*)&k_batch_fwd<T, 64, MODE>;
     k.adj = (const void*)&k_batch_adj<T, 64>;
+  } else if (bk == 16) {
+    k.fwd = (const void*)&k_batch_fwd<T, 16, MODE>;
+    k.adj = (const void*)&k_batch_adj<T, 16>;
   } else {
     k.fwd = (const void*)&k_batch_fwd<T, 32, MODE>;
     k.adj = (const void*)&k_batch_adj<T, 32>;
@@ -178,7 +183,8 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     return set_error(ADT_EINVAL, "batch: ref_compat needs ADT_F64");
   if (o.max_iter < 1 || o.adj_max_iter < 1 || !(o.tol >= 0.0))
     return set_error(ADT_EINVAL, "batch: bad iteration caps or tolerance");
-  if (o.bk != 0 && o.bk != 32 && o.bk != 64) return set_error(ADT_EINVAL, "batch: bk must be 0, 32 or 64");
+  if (o.bk != 0 && o.bk != 16 && o.bk != 32 && o.bk != 64)
+    return set_error(ADT_EINVAL, "batch: bk must be 0, 16, 32 or 64");
   auto P = std::make_unique<BatchPlan>();
   P->opts = o;
   if (o.ref_compat) P->opts.max_iter = std::min(o.max_iter, 20);

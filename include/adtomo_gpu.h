@@ -160,7 +160,7 @@ typedef struct adt_batch_opts {
                            box update in FP64 (default 2; -1 disables) */
   int32_t chunk;        /* solves resident at once; forward fields are recomputed
                            per chunk (0 = all solves at once) */
-  int32_t bk;           /* brick depth along k: 0 = default (32), else 32 or 64 */
+  int32_t bk;           /* brick depth along k: 0 = default (32), else 16, 32 or 64 */
   int32_t warps;        /* warps per solve (one warp group per solve): 0 = default */
   int32_t groups;       /* solves resident per CTA (warp groups): 0 = as many as fit */
   int32_t use_graph;    /* 1 (default): replay the evaluation as a CUDA graph */

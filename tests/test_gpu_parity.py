@@ -246,7 +246,7 @@ def test_batch_chunking_and_graph_do_not_change_results():
     fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 7, 6)
     ref = A.Batch3D(fields, stations, sf, src, use_graph=False)
     r = ref.run(slow, t_obs, w)
-    for kw in ({"chunk": 3}, {"chunk": 1, "use_graph": True}, {"bk": 64}, {"warps": 3},
+    for kw in ({"chunk": 3}, {"chunk": 1, "use_graph": True}, {"bk": 64}, {"bk": 16}, {"warps": 3},
                {"warps": 1, "groups": 1}, {"warps": 2, "groups": 5}):
         B = A.Batch3D(fields, stations, sf, src, **kw)
         out = B.run(slow, t_obs, w)
