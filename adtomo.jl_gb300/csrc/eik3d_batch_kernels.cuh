@@ -35,7 +35,8 @@ struct FieldDev {
   Geom g;
   double h;
   const T* f;               // slowness, compute precision
-  const double* f64;        // slowness, FP64 (near-source initial values, gradient)
+  const double* f64;        // slowness, FP64 (gradient)
+  const double* f0;         // slowness for the near-source initial values, FP64
   const uint32_t* bricks;   // level-ordered bricks
   const int* lstart;        // nlev + 1
   const double* sta;        // receivers, 3 per station
@@ -132,28 +133,68 @@ __device__ __forceinline__ double from_ordered<double>(unsigned long long b) {
   return __longlong_as_double((long long)b);
 }
 
-// Does brick b need a sweep at time t?  (lanes 0..6 read the meta words)
-__device__ __forceinline__ bool brick_needed(const int* mod, const int* proc, const Geom& g,
-                                             const BrickPos& p, int lane) {
-  const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
+// Does brick (bx, by, bz) need a sweep at time t of its level?  It does if it
+// changed in its own last sweep, or a face neighbour changed after that.
+//
+// Every warp of the group evaluates this for the whole level while other
+// warps may already be sweeping bricks of the same level, and all must get
+// the same answer.  Face neighbours lie in the levels before and after, which
+// do not change during the level.  The brick's own words are written only by
+// the warp that sweeps it, and only after that warp found it dirty: it sets
+// proc = t, then mod = t if something changed.  A reader sees either the old
+// words (dirty, as the sweeper found), proc == t (dirty by the first test) or
+// the old proc with mod == t (dirty by the second), so the answer is the same.
+__device__ __forceinline__ bool brick_dirty(const int* mod_, const int* proc_, const Geom& g,
+                                            int bx, int by, int bz, int t) {
+  const volatile int* mod = mod_;
+  const volatile int* proc = proc_;
+  const int b = (bx * g.nby + by) * g.nbz + bz;
   const int pr = proc[b];
-  int nb = -1;
-  switch (lane) {
-    case 0: nb = b; break;
-    case 1: nb = (p.bx > 0) ? b - g.nby * g.nbz : -1; break;
-    case 2: nb = (p.bx < g.nbx - 1) ? b + g.nby * g.nbz : -1; break;
-    case 3: nb = (p.by > 0) ? b - g.nbz : -1; break;
-    case 4: nb = (p.by < g.nby - 1) ? b + g.nbz : -1; break;
-    case 5: nb = (p.bz > 0) ? b - 1 : -1; break;
-    case 6: nb = (p.bz < g.nbz - 1) ? b + 1 : -1; break;
-    default: break;
+  if (pr == t) return true;
+  bool v = mod[b] >= pr;
+  const int sx = g.nby * g.nbz;
+  if (bx > 0) v |= mod[b - sx] > pr;
+  if (bx < g.nbx - 1) v |= mod[b + sx] > pr;
+  if (by > 0) v |= mod[b - g.nbz] > pr;
+  if (by < g.nby - 1) v |= mod[b + g.nbz] > pr;
+  if (bz > 0) v |= mod[b - 1] > pr;
+  if (bz < g.nbz - 1) v |= mod[b + 1] > pr;
+  return v;
+}
+
+// Run body(p) on this warp's share of the dirty bricks of the level
+// [q0, q1) of the level list.  Each warp forms the level's dirty mask itself
+// (one lane per brick, 32 bricks at a time) and takes the dirty bricks of
+// rank gw, gw + GW, ...: the group's warps get equal shares of the work
+// however the dirty bricks are spread over the level, without a barrier.
+template <int BK, class Body>
+__device__ __forceinline__ void for_dirty_bricks(const int* mod, const int* proc, const Geom& g,
+                                                 const uint32_t* __restrict__ bricks, int q0,
+                                                 int q1, int t, int si, int sj, int sk, int gw,
+                                                 int GW, int lane, Body&& body) {
+  int slot = 0;
+  for (int c0 = q0; c0 < q1; c0 += 32) {
+    const int qq = c0 + lane;
+    uint32_t packed = 0;
+    bool dv = false;
+    if (qq < q1) {
+      packed = bricks[qq];
+      int rx, ry, rz;
+      unpack_brick(packed, rx, ry, rz);
+      const int bx = si > 0 ? rx : g.nbx - 1 - rx;
+      const int by = sj > 0 ? ry : g.nby - 1 - ry;
+      const int bz = sk > 0 ? rz : g.nbz - 1 - rz;
+      dv = brick_dirty(mod, proc, g, bx, by, bz, t);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, dv);
+    while (m) {
+      const int bit = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t pk = __shfl_sync(0xffffffffu, packed, bit);
+      if (slot == gw) body(brick_pos<BK>(g, pk, si, sj, sk));
+      if (++slot == GW) slot = 0;
+    }
   }
-  bool v = false;
-  if (nb >= 0) {
-    const int md = mod[nb];
-    v = (lane == 0) ? (md >= pr) : (md > pr);
-  }
-  return __any_sync(0xffffffffu, v);
 }
 
 // ------------------------------------------------------------------ forward
@@ -202,27 +243,31 @@ __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx&
   return q < A.n_solves ? q : -1;
 }
 
-// Select the sweep instantiation for the ordering's tile stride, k direction
-// and near-source flag.
+// Select the sweep instantiation for the ordering's directions and the
+// near-source flag.
+template <int BK, int SI, int SJ, int SKD>
+__device__ __forceinline__ bool fwd_f32_dir(float* S, const float* F, const BrickPos& p, bool nr,
+                                            float h, double hd, const NearBox& box, int lane,
+                                            float& md) {
+  return nr ? sweep_brick_fwd_f32<BK, SI, SJ, SKD, true>(S, F, p, h, hd, box, lane, md)
+            : sweep_brick_fwd_f32<BK, SI, SJ, SKD, false>(S, F, p, h, hd, box, lane, md);
+}
+
 template <int BK>
 __device__ __forceinline__ bool dispatch_fwd_f32(float* S, const float* F, const BrickPos& p,
                                                  int si, int sj, int sk, bool nr, float h,
                                                  double hd, const NearBox& box, int lane,
                                                  float& md) {
-  constexpr int C9 = tile_col_stride(BK, true), C7 = tile_col_stride(BK, false);
-  const bool same = (sj == sk);
-  if (sk > 0) {
-    if (same)
-      return nr ? sweep_brick_fwd_f32<BK, C9, true, true>(S, F, p, si, sj, h, hd, box, lane, md)
-                : sweep_brick_fwd_f32<BK, C9, true, false>(S, F, p, si, sj, h, hd, box, lane, md);
-    return nr ? sweep_brick_fwd_f32<BK, C7, true, true>(S, F, p, si, sj, h, hd, box, lane, md)
-              : sweep_brick_fwd_f32<BK, C7, true, false>(S, F, p, si, sj, h, hd, box, lane, md);
+  switch ((si < 0) | ((sj < 0) << 1) | ((sk < 0) << 2)) {
+    case 0: return fwd_f32_dir<BK, 1, 1, 1>(S, F, p, nr, h, hd, box, lane, md);
+    case 1: return fwd_f32_dir<BK, -1, 1, 1>(S, F, p, nr, h, hd, box, lane, md);
+    case 2: return fwd_f32_dir<BK, 1, -1, 1>(S, F, p, nr, h, hd, box, lane, md);
+    case 3: return fwd_f32_dir<BK, -1, -1, 1>(S, F, p, nr, h, hd, box, lane, md);
+    case 4: return fwd_f32_dir<BK, 1, 1, -1>(S, F, p, nr, h, hd, box, lane, md);
+    case 5: return fwd_f32_dir<BK, -1, 1, -1>(S, F, p, nr, h, hd, box, lane, md);
+    case 6: return fwd_f32_dir<BK, 1, -1, -1>(S, F, p, nr, h, hd, box, lane, md);
+    default: return fwd_f32_dir<BK, -1, -1, -1>(S, F, p, nr, h, hd, box, lane, md);
   }
-  if (same)
-    return nr ? sweep_brick_fwd_f32<BK, C9, false, true>(S, F, p, si, sj, h, hd, box, lane, md)
-              : sweep_brick_fwd_f32<BK, C9, false, false>(S, F, p, si, sj, h, hd, box, lane, md);
-  return nr ? sweep_brick_fwd_f32<BK, C7, false, true>(S, F, p, si, sj, h, hd, box, lane, md)
-            : sweep_brick_fwd_f32<BK, C7, false, false>(S, F, p, si, sj, h, hd, box, lane, md);
 }
 
 template <class T, int BK, int MODE>
@@ -253,8 +298,20 @@ __global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
       T* uc = u + col * g.l;
       for (int k = lane; k < g.l; k += 32) uc[k] = (T)u0_at(sd, i, j, k);
     }
+    // Only the bricks whose cells or halo hold a source node start dirty.
+    // Every other cell starts at 1000 with all its neighbours at 1000, and
+    // with f h > 0 no candidate falls below 1000, so such a brick cannot
+    // change until a neighbour does: skipping it is exact, like every other
+    // skip.  (The halo counts: a brick next to a source node changes in its
+    // first sweep even while the source's own brick has not been swept.)
+    auto near = [](int x0, int x1, int b, int B) {
+      return (x0 >= b * B - 1 && x0 <= b * B + B) || (x1 >= b * B - 1 && x1 <= b * B + B);
+    };
     for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
-      mod[b] = -1;
+      const int bx = b / (g.nby * g.nbz), by = (b / g.nbz) % g.nby, bz = b % g.nbz;
+      const bool src = near(sd.xf, sd.xc, bx, BI) && near(sd.yf, sd.yc, by, BJ) &&
+                       near(sd.zf, sd.zc, bz, BK);
+      mod[b] = src ? -1 : -2;
       proc[b] = -1;
     }
     NearBox box;
@@ -283,10 +340,8 @@ __global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
         const int CS = tile_col_stride(BK, sj == sk);
         for (int d = 0; d < g.nlev; ++d) {
           const int t = (it * 8 + o) * g.nlev + d;
-          const int q1 = fd.lstart[d + 1];
-          for (int qq = fd.lstart[d] + c.gw; qq < q1; qq += c.GW) {
-            const BrickPos p = brick_pos<BK>(g, fd.bricks[qq], si, sj, sk);
-            if (!brick_needed(mod, proc, g, p, lane)) continue;
+          for_dirty_bricks<BK>(mod, proc, g, fd.bricks, fd.lstart[d], fd.lstart[d + 1], t, si, sj,
+                               sk, c.gw, c.GW, lane, [&](const BrickPos& p) {
             bool ch;
             if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
               if (vec) {
@@ -322,7 +377,7 @@ __global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
               cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
               cnt_brk += 1;
             }
-          }
+          });
           group_sync(c.grp, c.gthreads);
         }
       }
@@ -525,12 +580,16 @@ __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const
                                                  const int64_t* sidx, const float* sval,
                                                  int ns, const Geom& g, const BrickPos& p, int si,
                                                  int sj, int sk, int lane) {
-  constexpr int C9 = tile_col_stride(BK, true), C7 = tile_col_stride(BK, false);
-  if (sk > 0)
-    return (sj == sk) ? sweep_brick_adj_f32<BK, C9, true>(U, L, C, sidx, sval, ns, g, p, si, sj, lane)
-                      : sweep_brick_adj_f32<BK, C7, true>(U, L, C, sidx, sval, ns, g, p, si, sj, lane);
-  return (sj == sk) ? sweep_brick_adj_f32<BK, C9, false>(U, L, C, sidx, sval, ns, g, p, si, sj, lane)
-                    : sweep_brick_adj_f32<BK, C7, false>(U, L, C, sidx, sval, ns, g, p, si, sj, lane);
+  switch ((si < 0) | ((sj < 0) << 1) | ((sk < 0) << 2)) {
+    case 0: return sweep_brick_adj_f32<BK, 1, 1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 1: return sweep_brick_adj_f32<BK, -1, 1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 2: return sweep_brick_adj_f32<BK, 1, -1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 3: return sweep_brick_adj_f32<BK, -1, -1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 4: return sweep_brick_adj_f32<BK, 1, 1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 5: return sweep_brick_adj_f32<BK, -1, 1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 6: return sweep_brick_adj_f32<BK, 1, -1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
+    default: return sweep_brick_adj_f32<BK, -1, -1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
+  }
 }
 
 template <class T, int BK>
@@ -628,15 +687,13 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
         const int CS = tile_col_stride(BK, sj == sk);
         for (int d = 0; d < g.nlev; ++d) {
           const int t = (it * 8 + o) * g.nlev + d;
-          const int q1 = fd.lstart[d + 1];
-          for (int qq = fd.lstart[d] + c.gw; qq < q1; qq += c.GW) {
-            const BrickPos p = brick_pos<BK>(g, fd.bricks[qq], si, sj, sk);
-            if (!brick_needed(mod, proc, g, p, lane)) continue;
+          for_dirty_bricks<BK>(mod, proc, g, fd.bricks, fd.lstart[d], fd.lstart[d + 1], t, si, sj,
+                               sk, c.gw, c.GW, lane, [&](const BrickPos& p) {
             bool ch;
             if constexpr (sizeof(T) == 4) {
               if (vec) {
                 load_tile_f32_vec<BK>(U, u, g, p, CS, lane);
-                load_tile_f32_vec<BK>(L, lam, g, p, CS, lane);
+                load_tile_f32_vec<BK>(L, lam, g, p, CS, lane, 0.0f);
                 load_codes_vec<BK>(C, code, g, p, CS, lane);
                 __syncwarp();
                 ch = dispatch_adj_f32<BK>(U, L, C, sidx, sval, ns, g, p, si, sj, sk, lane);
@@ -670,7 +727,7 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
               cnt_brk += 1;
             }
             any |= ch;
-          }
+          });
           group_sync(c.grp, c.gthreads);
         }
       }

@@ -204,8 +204,10 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
 // of 4, so every brick column segment starts on a 16-byte boundary).  The 56
 // columns of a halo tile (32 interior, 24 face columns) are split into
 // 4-float chunks; lane t takes chunks t, t+32, ...  Out-of-grid cells of the
-// halo are written as +inf, so min(neighbour pair) falls back to the single
-// interior neighbour exactly as the reference's edge rule does.
+// halo are written as `ghost`: +inf for travel times, so min(neighbour pair)
+// falls back to the single interior neighbour exactly as the reference's edge
+// rule does, and 0 for adjoint variables, whose ghosts are only ever
+// multiplied by a zero weight.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void halo_col(int c, int& ci, int& cj) {
   if (c < BI * BJ) {  // interior
@@ -230,13 +232,14 @@ constexpr int LOAD_BATCH = 7;
 template <int BK>
 __device__ __forceinline__ void load_tile_f32_vec(float* S, const float* __restrict__ src,
                                                   const Geom& g, const BrickPos& p, int CS,
-                                                  int lane) {
+                                                  int lane,
+                                                  float ghost = INFINITY) {
   constexpr int RS = tile_row_stride(BK);
   constexpr int CH = BK / 4;
   constexpr int NCOL = BI * BJ + 2 * BI + 2 * BJ;  // 56
   constexpr int PER = NCOL * CH / 32;              // chunks per lane (exact)
   static_assert(NCOL * CH % 32 == 0 && PER % LOAD_BATCH == 0, "tile chunking");
-  const float INF = __int_as_float(0x7f800000);
+  const float INF = ghost;
   // k halo of the interior columns (lane c takes interior column c), issued first
   const int hci = (lane >> 2) + 1, hcj = (lane & 3) + 1;
   float hlo = INF, hhi = INF;
@@ -378,57 +381,72 @@ __device__ __forceinline__ void sts_if(bool p, uint32_t a, float v) {
 
 // FP32 forward sweep of one staged brick (the batched path), for tiles
 // staged by load_tile_f32_vec (out-of-grid ghosts are +inf, so every
-// neighbour pair is a plain min).  Same data flow as sweep_brick_fwd; the k
-// neighbours are carried in registers: the upstream one is this lane's
-// previous result and the downstream one is loaded one step ahead and reused
-// as the next step's old value.  The step body is branch-free: lanes outside
-// their active window read a valid cell of their own column and only the
-// store and the carried state are predicated.  CS: column stride of the
-// ordering's tile layout; SKP: sweep runs towards +k.  NEAR: cells in the
-// source box update in FP64.
-template <int BK, int CS, bool SKP, bool NEAR>
+// neighbour pair is a plain min).  Same data flow as sweep_brick_fwd, as a
+// software pipeline.  At step tau the lane's cell is kk = tau - s; of its
+// neighbours only the two upstream ones across columns (x and y, written by
+// other lanes one step earlier) and the z-upstream one (this lane's own
+// previous result, kept in a register) are new.  The downstream neighbours
+// and the slowness cannot change before this step, so they are loaded one
+// step ahead, and each step's dependency path is just: two shared loads, the
+// local solve, the store.  Lanes outside their window [0, nk) run the same
+// code on cells of their own column extended past the brick (still inside
+// this warp's tiles, by the tile layout) and only the store is predicated:
+// the carried old value at kk = -1 is the halo cell, so the z-upstream value
+// entering the window is right without a special case.  SI, SJ, SKD: sweep
+// directions; NEAR: cells in the source box update in FP64.
+template <int BK, int SI, int SJ, int SKD, bool NEAR>
 __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, const BrickPos& p,
-                                                    int si, int sj, float h, double hd,
-                                                    const NearBox& nb, int lane, float& maxdec) {
+                                                    float h, double hd, const NearBox& nb,
+                                                    int lane, float& maxdec) {
   constexpr int RS = tile_row_stride(BK);
   constexpr int IRS = itile_row_stride(BK);
-  constexpr int SK = SKP ? 1 : -1;
+  constexpr int CS = tile_col_stride(BK, SJ == SKD);
+  constexpr int DZ = 4 * SKD;                       // bytes per step along the column
+  constexpr int XU = -4 * RS * SI, XD = 4 * RS * SI;  // byte offsets, upstream / downstream
+  constexpr int YU = -4 * CS * SJ, YD = 4 * CS * SJ;
   const int li = lane >> 2, lj = lane & 3;
-  const int pi = si > 0 ? li : BI - 1 - li;
-  const int pj = sj > 0 ? lj : BJ - 1 - lj;
+  const int pi = SI > 0 ? li : BI - 1 - li;
+  const int pj = SJ > 0 ? lj : BJ - 1 - lj;
   const int s = li + lj;
   const bool colok = (pi < p.ni) && (pj < p.nj);
   const int nk = colok ? p.nk : 0;
-  const int kb = SKP ? 0 : p.nk - 1;
-  const uint32_t a0 = smem_u32(S + (pi + 1) * RS + (pj + 1) * CS + 1 + kb);
-  const uint32_t fa0 = smem_u32(F + pi * IRS + pj * CS + kb);
-  float uo = lds<0>(a0);
-  float prev = lds<-4 * SK>(a0);
+  const int kb = SKD > 0 ? 0 : p.nk - 1;
+  // addresses of the lane's cell at tau = 0 (kk = -s)
+  uint32_t a = smem_u32(S + (pi + 1) * RS + (pj + 1) * CS + 1 + kb) - DZ * s;
+  uint32_t fa = smem_u32(F + pi * IRS + pj * CS + kb) - DZ * s;
+  float uo = lds<0>(a);      // old value of the cell
+  float prev = lds<-DZ>(a);  // value of the z-upstream cell
+  float dn = lds<DZ>(a), xd = lds<XD>(a), yd = lds<YD>(a);
+  float fc = lds<0>(fa);
   float mb = 0.0f;
   const int nsteps = p.nk + SKEW;
-#pragma unroll 2
+#pragma unroll 1
   for (int tau = 0; tau < nsteps; ++tau) {
     const int kk = tau - s;
     const bool act = (unsigned)kk < (unsigned)nk;
-    const int kc = act ? kk : 0;
-    const uint32_t a = a0 + (uint32_t)(4 * SK * kc);
-    const float dn = lds<4 * SK>(a);
-    const float xm = lds<-4 * RS>(a), xp = lds<4 * RS>(a);
-    const float ym = lds<-4 * CS>(a), yp = lds<4 * CS>(a);
-    const float fc = lds<0>(fa0 + (uint32_t)(4 * SK * kc));
+    const float xu = lds<XU>(a), yu = lds<YU>(a);
+    // next step's stable operands
+    const float n_dn = lds<2 * DZ>(a), n_xd = lds<XD + DZ>(a), n_yd = lds<YD + DZ>(a);
+    const float n_fc = lds<DZ>(fa);
     const float az = fminf(prev, dn);
-    const float ax = fminf(xm, xp);
-    const float ay = fminf(ym, yp);
+    const float ax = fminf(xu, xd);
+    const float ay = fminf(yu, yd);
     float un;
-    if (NEAR && act && nb.has(p.i0 + pi, p.j0 + pj, p.k0 + kb + SK * kc))
+    if (NEAR && act && nb.has(p.i0 + pi, p.j0 + pj, p.k0 + kb + SKD * kk))
       un = (float)upd3_stable<double>((double)ax, (double)ay, (double)az, (double)fc * hd);
     else
       un = upd3_f32(ax, ay, az, fc * h);
     const float d = act ? uo - un : 0.0f;
     sts_if(d > 0.0f, a, un);
     mb = fmaxf(mb, d);
-    prev = act ? fminf(un, uo) : prev;
-    uo = act ? dn : uo;
+    prev = d > 0.0f ? un : uo;
+    uo = dn;
+    dn = n_dn;
+    xd = n_xd;
+    yd = n_yd;
+    fc = n_fc;
+    a += DZ;
+    fa += DZ;
     __syncwarp();
   }
   maxdec = fmaxf(maxdec, mb);
@@ -483,76 +501,145 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return r;
 }
 
-// FP32 adjoint sweep of one staged brick (tiles from the vector loaders).
-// lambda_c = (g_c + 2 sum_users (u_r - u_c) lambda_r) / (2 sum_active (u_c - u_upwind)).
-// Branch-free: the six neighbours' u and lambda are loaded once and serve
-// both the user terms and the diagonal; inactive terms are selected away
-// (selects, not products, so +inf ghosts never turn into NaN).  U and L
-// share one tile layout at byte distance LOFF.  CS: column stride of the
-// ordering's layout; SKP: sweep runs towards +k.
-template <int BK, int CS, bool SKP>
+// Per-cell constants of one FP32 adjoint update, formed one step ahead.
+// The user terms w_q lambda_q (w_q = u_q - u_c for a user q, else 0) are
+// summed in one fixed order whatever the sweep direction:
+//   acc = (P_x + P_y) + P_z,  P_a = fma(w_{a+}, lambda_{a+}, w_{a-} lambda_{a-}),
+// so a cell evaluates to the same bits in every ordering and the sweeps
+// reach an exact fixed point (an order that followed the sweep would make
+// the orderings disagree in the last bit and never settle).  Per axis one
+// lambda is new in the sweep (the upstream neighbour) and one is old: when
+// the new one is the minus neighbour, P = fma(a, b, w_u lambda_u) with
+// (a, b) = (w_d, lambda_d); when it is the plus neighbour, P = fma(w_u,
+// lambda_u, a) with a = w_d lambda_d.  lambda = fma(acc, c2, c0).
+struct AdjCellF32 {
+  float wx, ax, bx, wy, ay, by, wz, az, bz;
+  float c2, c0;
+  bool wrok;  // active, not fixed
+};
+
+template <int S>
+__device__ __forceinline__ float adj_pair(float w_u, float l_u, float a, float b) {
+  return S > 0 ? fmaf(a, b, w_u * l_u) : fmaf(w_u, l_u, a);
+}
+
+// lambda_c = (g_c + 2 sum_users (u_r - u_c) lambda_r) / (2 sum_active (u_c - u_upwind))
+// for the cell with the given code and neighbours (xu/xd: upstream /
+// downstream along x for the sweep, likewise y and z).  Inactive terms are
+// selected away (selects, not products, so +inf ghosts never turn into NaN);
+// the adjoint tile's ghosts are 0, so their zero weights multiply zeros.
+template <int SI, int SJ, int SKD>
+__device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, float uxu, float uxd,
+                                                   float uyu, float uyd, float uzu, float uzd,
+                                                   float lxd, float lyd, float lzd, bool act,
+                                                   int64_t key, const int64_t* seed_idx,
+                                                   const float* seed_val, int n_seed) {
+  // user bits (absolute: x-, x+, y-, y+, z-, z+) and upwind side codes
+  // (1 minus, 2 plus) of the upstream / downstream neighbours of this sweep
+  constexpr uint32_t XU = SI > 0 ? 1u : 2u, XD = SI > 0 ? 2u : 1u;
+  constexpr uint32_t YU = SJ > 0 ? 4u : 8u, YD = SJ > 0 ? 8u : 4u;
+  constexpr uint32_t ZU = SKD > 0 ? 16u : 32u, ZD = SKD > 0 ? 32u : 16u;
+  constexpr uint32_t SXU = SI > 0 ? 1u : 2u, SYU = SJ > 0 ? 1u : 2u, SZU = SKD > 0 ? 1u : 2u;
+  const uint32_t us = code >> CODE_USERS;
+  AdjCellF32 c;
+  c.wx = (us & XU) ? uxu - uc : 0.0f;
+  c.wy = (us & YU) ? uyu - uc : 0.0f;
+  c.wz = (us & ZU) ? uzu - uc : 0.0f;
+  const float w_xd = (us & XD) ? uxd - uc : 0.0f;
+  const float w_yd = (us & YD) ? uyd - uc : 0.0f;
+  const float w_zd = (us & ZD) ? uzd - uc : 0.0f;
+  if (SI > 0) { c.ax = w_xd; c.bx = lxd; } else { c.ax = w_xd * lxd; c.bx = 0.0f; }
+  if (SJ > 0) { c.ay = w_yd; c.by = lyd; } else { c.ay = w_yd * lyd; c.by = 0.0f; }
+  if (SKD > 0) { c.az = w_zd; c.bz = lzd; } else { c.az = w_zd * lzd; c.bz = 0.0f; }
+  const uint32_t sx = code & 3u, sy = (code >> 2) & 3u, sz = (code >> 4) & 3u;
+  float d = sx ? uc - (sx == SXU ? uxu : uxd) : 0.0f;
+  d += sy ? uc - (sy == SYU ? uyu : uyd) : 0.0f;
+  d += sz ? uc - (sz == SZU ? uzu : uzd) : 0.0f;
+  float gs = 0.0f;
+  if (act && (code & CODE_SEED)) {
+    int lo = 0, hi = n_seed - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (seed_idx[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    gs = seed_val[lo];
+  }
+  c.c2 = rcp_approx(d);
+  c.c0 = 0.5f * gs * c.c2;
+  c.wrok = act && !(code & CODE_FIXED);
+  return c;
+}
+
+// FP32 adjoint sweep of one staged brick (tiles from the vector loaders), as a
+// software pipeline like sweep_brick_fwd_f32: u and the codes are read-only
+// during the sweep and the downstream adjoint values cannot change before the
+// step that reads them, so everything but the x and y upstream adjoint values
+// is loaded, and the cell's constants formed, one step ahead.  A step's
+// dependency path is two shared loads, at most five FMA-pipe operations and
+// the store.  U and L
+// share one tile layout; SI, SJ, SKD: sweep directions.
+template <int BK, int SI, int SJ, int SKD>
 __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, const uint16_t* C,
                                                     const int64_t* seed_idx, const float* seed_val,
                                                     int n_seed, const Geom& g, const BrickPos& p,
-                                                    int si, int sj, int lane) {
+                                                    int lane) {
   constexpr int RS = tile_row_stride(BK);
   constexpr int IRS = itile_row_stride(BK);
-  constexpr int SK = SKP ? 1 : -1;
+  constexpr int CS = tile_col_stride(BK, SJ == SKD);
+  constexpr int DZ = 4 * SKD, DC = 2 * SKD;
+  constexpr int XU = -4 * RS * SI, XD = 4 * RS * SI;
+  constexpr int YU = -4 * CS * SJ, YD = 4 * CS * SJ;
   const int li = lane >> 2, lj = lane & 3;
-  const int pi = si > 0 ? li : BI - 1 - li;
-  const int pj = sj > 0 ? lj : BJ - 1 - lj;
+  const int pi = SI > 0 ? li : BI - 1 - li;
+  const int pj = SJ > 0 ? lj : BJ - 1 - lj;
   const int s = li + lj;
   const bool colok = (pi < p.ni) && (pj < p.nj);
   const int nk = colok ? p.nk : 0;
-  const int kb = SKP ? 0 : p.nk - 1;
+  const int kb = SKD > 0 ? 0 : p.nk - 1;
   const int own = (pi + 1) * RS + (pj + 1) * CS + 1 + kb;
-  const uint32_t ua0 = smem_u32(U + own);
-  const uint32_t la0 = smem_u32(L + own);
-  const uint32_t ca0 = smem_u32(C + pi * IRS + pj * CS + kb);
+  // addresses of the lane's cell at tau = 0 (kk = -s)
+  uint32_t ua = smem_u32(U + own) - DZ * s;
+  uint32_t la = smem_u32(L + own) - DZ * s;
+  uint32_t ca = smem_u32(C + pi * IRS + pj * CS + kb) - DC * s;
   const int64_t gcol = ((int64_t)(p.i0 + pi) * g.n + (p.j0 + pj)) * g.l + p.k0 + kb;
+  float uc = lds<0>(ua), uzd = lds<DZ>(ua);
+  float lold = lds<0>(la), lzd = lds<DZ>(la);
+  float lzu = lds<-DZ>(la);
+  AdjCellF32 cur = adj_cell_f32<SI, SJ, SKD>(
+      ldsu16(ca), uc, lds<XU>(ua), lds<XD>(ua), lds<YU>(ua), lds<YD>(ua), lds<-DZ>(ua), uzd,
+      lds<XD>(la), lds<YD>(la), lzd, (unsigned)(-s) < (unsigned)nk, gcol - SKD * s, seed_idx,
+      seed_val, n_seed);
   bool changed = false;
   const int nsteps = p.nk + SKEW;
 #pragma unroll 1
   for (int tau = 0; tau < nsteps; ++tau) {
-    const int kk = tau - s;
-    const bool act = (unsigned)kk < (unsigned)nk;
-    const int kc = act ? kk : 0;
-    const uint32_t ua = ua0 + (uint32_t)(4 * SK * kc);
-    const uint32_t la = la0 + (uint32_t)(4 * SK * kc);
-    const uint32_t code = ldsu16(ca0 + (uint32_t)(2 * SK * kc));
-    const float uc = lds<0>(ua);
-    const float u_xm = lds<-4 * RS>(ua), u_xp = lds<4 * RS>(ua);
-    const float u_ym = lds<-4 * CS>(ua), u_yp = lds<4 * CS>(ua);
-    const float u_zm = lds<-4>(ua), u_zp = lds<4>(ua);
-    const float l_xm = lds<-4 * RS>(la), l_xp = lds<4 * RS>(la);
-    const float l_ym = lds<-4 * CS>(la), l_yp = lds<4 * CS>(la);
-    const float l_zm = lds<-4>(la), l_zp = lds<4>(la);
-    const float lold = lds<0>(la);
-    const uint32_t us = code >> CODE_USERS;
-    float acc = (us & 1u) ? (u_xm - uc) * l_xm : 0.0f;
-    acc += (us & 2u) ? (u_xp - uc) * l_xp : 0.0f;
-    acc += (us & 4u) ? (u_ym - uc) * l_ym : 0.0f;
-    acc += (us & 8u) ? (u_yp - uc) * l_yp : 0.0f;
-    acc += (us & 16u) ? (u_zm - uc) * l_zm : 0.0f;
-    acc += (us & 32u) ? (u_zp - uc) * l_zp : 0.0f;
-    const uint32_t sx = code & 3u, sy = (code >> 2) & 3u, sz = (code >> 4) & 3u;
-    float d = sx ? uc - (sx == 1u ? u_xm : u_xp) : 0.0f;
-    d += sy ? uc - (sy == 1u ? u_ym : u_yp) : 0.0f;
-    d += sz ? uc - (sz == 1u ? u_zm : u_zp) : 0.0f;
-    float gs = 0.0f;
-    if (act && (code & CODE_SEED)) {
-      const int64_t key = gcol + SK * kc;
-      int lo = 0, hi = n_seed - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (seed_idx[mid] < key) lo = mid + 1; else hi = mid;
-      }
-      gs = seed_val[lo];
-    }
-    const float lam = fmaf(2.0f, acc, gs) * rcp_approx(2.0f * d);
-    const bool wr = act && !(code & CODE_FIXED) && (lam != lold);
+    const float lxu = lds<XU>(la), lyu = lds<YU>(la);
+    // next cell's operands
+    const uint32_t n_code = ldsu16(ca + DC);
+    const float n_uxu = lds<DZ + XU>(ua), n_uxd = lds<DZ + XD>(ua);
+    const float n_uyu = lds<DZ + YU>(ua), n_uyd = lds<DZ + YD>(ua);
+    const float n_uzd = lds<2 * DZ>(ua);
+    const float n_lxd = lds<DZ + XD>(la), n_lyd = lds<DZ + YD>(la);
+    const float n_lzd = lds<2 * DZ>(la);
+    const float acc = (adj_pair<SI>(cur.wx, lxu, cur.ax, cur.bx) +
+                       adj_pair<SJ>(cur.wy, lyu, cur.ay, cur.by)) +
+                      adj_pair<SKD>(cur.wz, lzu, cur.az, cur.bz);
+    const float lam = fmaf(acc, cur.c2, cur.c0);
+    const bool wr = cur.wrok && (lam != lold);
     sts_if(wr, la, lam);
     changed |= wr;
+    lzu = wr ? lam : lold;
+    const int kn = tau + 1 - s;
+    cur = adj_cell_f32<SI, SJ, SKD>(n_code, uzd, n_uxu, n_uxd, n_uyu, n_uyd, uc, n_uzd, n_lxd,
+                                    n_lyd, n_lzd, (unsigned)kn < (unsigned)nk, gcol + SKD * kn,
+                                    seed_idx, seed_val, n_seed);
+    uc = uzd;
+    uzd = n_uzd;
+    lold = lzd;
+    lzd = n_lzd;
+    ua += DZ;
+    la += DZ;
+    ca += DC;
     __syncwarp();
   }
   return __any_sync(0xffffffffu, changed);
