@@ -78,11 +78,14 @@ SIGNATURES = {
     "adt_batch_destroy": (C.c_int, [_P]),
     "adt_batch_run": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "adt_batch_upload": (C.c_int, [_P, _P, _P, _P]),
+    "adt_batch_set_source_slowness": (C.c_int, [_P, _P]),
     "adt_batch_run_resident": (C.c_int, [_P]),
     "adt_batch_download": (C.c_int, [_P, _P, _P, _P, _P]),
     "adt_batch_stream": (_P, [_P]),
     "adt_batch_device_buffer": (_P, [_P, _I32]),
     "adt_batch_stats_get": (C.c_int, [_P, _P]),
+    "adt_smooth_l1": (C.c_int, [_P, _I64, _I64, _I64, _I32, _I32, _D, _P, _P]),
+    "adt_smooth_l1_device": (C.c_int, [_P, _I64, _I64, _I64, _I32, _I32, _D, _P, _P, _P]),
 }
 
 

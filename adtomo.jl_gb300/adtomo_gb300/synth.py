@@ -35,7 +35,7 @@ def layered_smooth(m, n, l, rng, amp=0.05, v_top=4.0, v_bot=8.0, corr=6.0):
     ky = np.fft.fftfreq(n)[None, :, None]
     kz = np.fft.rfftfreq(l)[None, None, :]
     spec *= np.exp(-2 * (np.pi * corr) ** 2 * (kx ** 2 + ky ** 2 + kz ** 2))
-    sm = np.fft.irfftn(spec, s=(m, n, l))
+    sm = np.fft.irfftn(spec, s=(m, n, l), axes=(0, 1, 2))
     sm /= max(np.abs(sm).max(), 1e-30)
     return v[None, None, :] * (1.0 + amp * sm)
 

@@ -301,6 +301,11 @@ int adt_batch_upload(adt_batch* b, const double* slowness, const double* t_obs,
   return batch_upload(b->plan, slowness, t_obs, weight);
 }
 
+int adt_batch_set_source_slowness(adt_batch* b, const double* slowness0) {
+  if (!b) return set_error(ADT_EINVAL, "batch: null handle");
+  return batch_set_source_slowness(b->plan, slowness0);
+}
+
 int adt_batch_run_resident(adt_batch* b) {
   if (!b) return set_error(ADT_EINVAL, "batch: null handle");
   return batch_run_resident(b->plan);

@@ -29,7 +29,7 @@ __global__ void k_to_t_f32(const double* __restrict__ a, float* __restrict__ b, 
 // FP64 near-source initial values: sqrt(dx^2+dy^2+dz^2) * f * h at the 8
 // nodes around each source (scripts/gene_obs.jl:44-51, order ceil/floor).
 template <class T>
-__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields) {
+__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields, int fixed) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   SolveDev& sd = solves[s];
@@ -42,7 +42,8 @@ __global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields) {
         const int64_t p = ((int64_t)xs[a] * fd.g.n + ys[b]) * fd.g.l + zs[c];
         const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                               __dmul_rn(dz, dz)));
-        sd.v0[a * 4 + b * 2 + c] = __dmul_rn(__dmul_rn(r, fd.f64[p]), fd.h);
+        const double f = fixed ? fd.f0[p] : fd.f64[p];
+        sd.v0[a * 4 + b * 2 + c] = __dmul_rn(__dmul_rn(r, f), fd.h);
       }
 }
 
@@ -130,10 +131,11 @@ struct BatchPlan {
   };
   std::vector<Chunk> chunks;
   // device
-  DevBuf d_slow64, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
+  DevBuf d_slow64, d_slow0, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
   DevBuf d_levels, d_lstart, d_fields, d_solves, d_order, d_uoff;
   DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
   int64_t snap_stride = 0;
+  bool src_fixed = false;  // near-source values from d_slow0 (batch_set_source_slowness)
   // launch shapes
   KernelSet ks;
   int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
@@ -299,6 +301,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
 #define R_(b, n) \
   if ((rc = R(b, n))) return rc;
   R_(P->d_slow64, P->ncell_total * 8);
+  R_(P->d_slow0, P->ncell_total * 8);
   R_(P->d_slowT, P->f64 ? 16 : P->ncell_total * 4);
   R_(P->d_sta, (size_t)sofs * 3 * 8);
   R_(P->d_tobs, P->nobs * 8);
@@ -343,6 +346,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].g = P->geoms[f];
       fdv[f].h = P->h[f];
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
+      fdv[f].f0 = P->d_slow0.as<double>() + P->cell_off[f];
       fdv[f].f = fdv[f].f64;
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
@@ -358,6 +362,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].g = P->geoms[f];
       fdv[f].h = P->h[f];
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
+      fdv[f].f0 = P->d_slow0.as<double>() + P->cell_off[f];
       fdv[f].f = P->d_slowT.as<float>() + P->cell_off[f];
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
@@ -492,7 +497,8 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
     k_to_t_f32<<<grid1d(P.ncell_total), 256, 0, st>>>(P.d_slow64.as<double>(), P.d_slowT.as<float>(),
                                                       P.ncell_total);
   k_src_init<T><<<(P.ns + 127) / 128, 128, 0, st>>>(P.d_solves.as<SolveDev>(), P.ns,
-                                                     P.d_fields.as<FieldDev<T>>());
+                                                     P.d_fields.as<FieldDev<T>>(),
+                                                     P.src_fixed ? 1 : 0);
   ADT_CUDA(cudaMemsetAsync(P.d_grad.p, 0, P.ncell_total * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_next.p, 0, 2 * P.chunks.size() * 4, st));
@@ -556,6 +562,24 @@ int batch_upload(BatchPlan* P, const double* slowness, const double* t_obs, cons
   }
   if (t_obs) ADT_CUDA(cudaMemcpyAsync(P->d_tobs.p, t_obs, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
   if (weight) ADT_CUDA(cudaMemcpyAsync(P->d_w.p, weight, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
+  return ADT_OK;
+}
+
+int batch_set_source_slowness(BatchPlan* P, const double* slowness0) {
+  if (slowness0) {
+    for (int64_t i = 0; i < P->ncell_total; ++i)
+      if (!(slowness0[i] > 0.0) || !std::isfinite(slowness0[i]))
+        return set_error(ADT_EINVAL, "batch: source slowness must be finite and > 0 (cell %lld)",
+                         (long long)i);
+    ADT_CUDA(cudaMemcpyAsync(P->d_slow0.p, slowness0, P->ncell_total * 8, cudaMemcpyHostToDevice,
+                             P->stream));
+  }
+  ADT_CUDA(cudaStreamSynchronize(P->stream));
+  if (P->src_fixed != (slowness0 != nullptr) && P->graph) {  // the source kernel's argument changes
+    cudaGraphExecDestroy(P->graph);
+    P->graph = nullptr;
+  }
+  P->src_fixed = slowness0 != nullptr;
   return ADT_OK;
 }
 

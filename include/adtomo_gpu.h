@@ -182,6 +182,15 @@ int adt_batch_destroy(adt_batch* b);
 int adt_batch_run(adt_batch* b, const double* slowness, const double* t_obs, const double* weight,
                   double* misfit, double* t_pred, double* grad, adt_solve_status* status);
 
+/* Slowness used for the near-source initial values (the 8 nodes around each
+ * source get distance * h * slowness).  By default that is the slowness of
+ * the evaluation itself.  scripts/inversion.jl:52-60 instead builds u0 from
+ * the starting model vel0 and keeps it while the model changes: pass that
+ * model's slowness here (all fields, as in adt_batch_run) to do the same.
+ * NULL returns to the default.  The near-source values are constants of the
+ * evaluation either way: the gradient does not flow through them. */
+int adt_batch_set_source_slowness(adt_batch* b, const double* slowness0);
+
 /* Device-resident use: upload inputs once, run, read outputs later.  upload
  * takes host pointers (NULL leaves that input unchanged); run_resident enqueues
  * one evaluation on the plan's stream without synchronising; download copies
@@ -214,6 +223,21 @@ typedef struct adt_batch_stats {
   int32_t ctas;
 } adt_batch_stats;
 int adt_batch_stats_get(adt_batch* b, adt_batch_stats* out);
+
+/* ------------------------------------------------------------------------
+ * Smoothness penalty of the inversion (replaces the TF graph of
+ * scripts/inversion.jl:107-121): penalty = lambda * sum |v - S v| over the
+ * m x n x l model v (C order), S the mean over an sh x sh x sv box centred
+ * on each cell with circular wrap-around (the reference's tf.concat padding +
+ * VALID conv3d).  grad (may be NULL) receives lambda * (s - S s), s =
+ * sign(v - S v): the gradient of the penalty with respect to v.  sh and sv
+ * are odd; (sh-1)/2 <= m, n and (sv-1)/2 <= l.  FP64 throughout; the sum is
+ * reduced in a fixed order, so repeated calls give identical results. */
+int adt_smooth_l1(const double* v, int64_t m, int64_t n, int64_t l, int32_t sh, int32_t sv,
+                  double lambda, double* penalty, double* grad);
+/* The same on device pointers (penalty: one device double), on `stream`. */
+int adt_smooth_l1_device(const double* v, int64_t m, int64_t n, int64_t l, int32_t sh,
+                         int32_t sv, double lambda, double* penalty, double* grad, void* stream);
 
 #ifdef __cplusplus
 }

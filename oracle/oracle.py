@@ -248,3 +248,24 @@ def ref_eik3d_backward(grad_u, u, u0, f, h):
     ref_lib().ref_eik3d_backward(gu0.ravel(), gf.ravel(), _c(grad_u).ravel(), u.ravel(),
                                  _c(u0).ravel(), _c(f).ravel(), float(h), m, n, l)
     return gu0, gf
+
+
+def smooth_l1(v, sh, sv, lam=1.0):
+    """lam * sum |v - S v| and its gradient lam * (s - S s), s = sign(v - S v),
+    S the circular box mean over sh x sh x sv cells: the penalty of
+    scripts/inversion.jl:107-121 (the tf.concat wrap-around padding followed by
+    a VALID conv3d with weights 1/(sh*sh*sv)).  Plain NumPy, FP64."""
+    v = np.asarray(v, np.float64)
+    rh, rv = (sh - 1) // 2, (sv - 1) // 2
+
+    def box(a):
+        out = np.zeros_like(a)
+        for dx in range(-rh, rh + 1):
+            for dy in range(-rh, rh + 1):
+                for dz in range(-rv, rv + 1):
+                    out += np.roll(a, (-dx, -dy, -dz), axis=(0, 1, 2))
+        return out / (sh * sh * sv)
+
+    r = v - box(v)
+    s = np.sign(r)
+    return lam * np.abs(r).sum(), lam * (s - box(s))

@@ -276,3 +276,42 @@ def test_batch_rejects_bad_geometry():
         A.Batch3D([(10, 10, 10, 1.0)], [np.zeros((1, 3))], [0], [[-0.5, 1.0, 1.0]])
     with pytest.raises(A.AdtError):
         A.Batch3D([(10, 10, 10, 1.0)], [np.zeros((1, 3))], [1], [[1.0, 1.0, 1.0]])
+
+
+def test_batch_c4_multi_field_uneven_grids():
+    """The C4 layout at reduced size: four grids of different sizes, each with
+    a P and an S field (Vs = Vp / 1.73, layered + smooth random), every event
+    solved on both fields; FP32 plan against the FP64 oracle, gradients with
+    respect to all eight slownesses."""
+    rng = np.random.default_rng(11)
+    grids = [(16, 16, 8, 0.5), (24, 24, 12, 0.5), (32, 32, 16, 0.5), (40, 40, 20, 0.5)]
+    fields, stations, slow = [], [], []
+    for (m, n, l, h) in grids:
+        vp = synth.layered_smooth(m, n, l, rng, corr=3.0)
+        sta = synth.surface_stations(m, n, 12, rng)
+        for v in (vp, vp / 1.73):
+            fields.append((m, n, l, h))
+            slow.append(1.0 / v)
+            stations.append(sta)
+    sf, src = [], []
+    for gi, (m, n, l, _) in enumerate(grids):
+        for e in synth.volume_sources(m, n, l, 3, rng):
+            for ph in range(2):
+                sf.append(2 * gi + ph)
+                src.append(e)
+    sf, src = np.array(sf), np.array(src)
+    n_obs = sum(len(stations[f]) for f in sf)
+    t_obs = rng.uniform(0.5, 3.0, n_obs)
+    t_obs[rng.random(n_obs) < 0.1] = -1.0
+    w = rng.uniform(0.5, 1.0, n_obs)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4
+    assert abs(mis - mo) <= 1e-3 * mo
+    assert len(grads) == 8
+    for g, r in zip(grads, go):
+        assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
+    assert all(s.converged and s.adj_converged for s in st)
+    B.close()
