@@ -134,7 +134,9 @@ struct BatchPlan {
   DevBuf d_slow64, d_slow0, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
   DevBuf d_levels, d_lstart, d_fields, d_solves, d_order, d_uoff;
   DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
+  DevBuf d_gdense;  // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
   int64_t snap_stride = 0;
+  std::vector<adt_solve_status> h_status;
   bool src_fixed = false;  // near-source values from d_slow0 (batch_set_source_slowness)
   // launch shapes
   KernelSet ks;
@@ -274,7 +276,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       P->solves[s].seed_off = seeds;
       ch.field_uoff[P->solve_field[s]].push_back(cells);
       cells += g.ncell;
-      bricks += 2LL * g.nbx * g.nby * g.nbz;
+      bricks += (int64_t)META_ARRAYS * g.nbx * g.nby * g.nbz;
       seeds += 8LL * P->nsta[P->solve_field[s]];
     }
     max_cells = std::max(max_cells, cells);
@@ -320,6 +322,10 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   R_(P->d_meta, (size_t)max_bricks * 4);
   R_(P->d_sidx, (size_t)std::max<int64_t>(max_seeds, 1) * 8);
   R_(P->d_sval, (size_t)std::max<int64_t>(max_seeds, 1) * es);
+  if (!P->f64) {
+    R_(P->d_gdense, (size_t)max_cells * es);
+    ADT_CUDA(cudaMemset(P->d_gdense.p, 0, (size_t)max_cells * es));
+  }
   R_(P->d_nseed, (size_t)n_solves * 4);
   R_(P->d_next, (size_t)2 * P->chunks.size() * 4);
   R_(P->d_counters, 4 * 8);
@@ -392,7 +398,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   const size_t fw = P->f64 ? fwd_warp_smem<double>(P->bk) : fwd_warp_smem<float>(P->bk);
   const size_t aw = P->f64 ? adj_warp_smem<double>(P->bk) : adj_warp_smem<float>(P->bk);
   for (auto& g : P->geoms) P->max_nb = std::max(P->max_nb, g.nbx * g.nby * g.nbz);
-  P->meta_smem = (2 * (size_t)P->max_nb * sizeof(int) <= 16384) ? 1 : 0;
+  P->meta_smem = ((size_t)META_ARRAYS * P->max_nb * sizeof(int) <= 16384) ? 1 : 0;
   cudaFuncAttributes fa_f, fa_a;
   ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
   ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
@@ -471,6 +477,7 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.meta = P.d_meta.as<int>();
   A.seed_idx = P.d_sidx.as<int64_t>();
   A.seed_val = P.d_sval.as<T>();
+  A.gdense = P.f64 ? nullptr : P.d_gdense.as<T>();
   A.n_seed = P.d_nseed.as<int>();
   A.snap = P.opts.ref_compat ? P.d_snap.as<T>() : nullptr;
   A.snap_stride = P.snap_stride;
@@ -614,10 +621,11 @@ int batch_download(BatchPlan* P, double* misfit, double* t_pred, double* grad,
   if (misfit) ADT_CUDA(cudaMemcpyAsync(misfit, P->d_mis.p, 8, cudaMemcpyDeviceToHost, P->stream));
   if (t_pred) ADT_CUDA(cudaMemcpyAsync(t_pred, P->d_tpred.p, P->nobs * 8, cudaMemcpyDeviceToHost, P->stream));
   if (grad) ADT_CUDA(cudaMemcpyAsync(grad, P->d_grad.p, P->ncell_total * 8, cudaMemcpyDeviceToHost, P->stream));
-  if (status)
-    ADT_CUDA(cudaMemcpyAsync(status, P->d_status.p, P->ns * sizeof(adt_solve_status), cudaMemcpyDeviceToHost,
-                             P->stream));
+  P->h_status.resize(P->ns);
+  ADT_CUDA(cudaMemcpyAsync(P->h_status.data(), P->d_status.p, P->ns * sizeof(adt_solve_status),
+                           cudaMemcpyDeviceToHost, P->stream));
   ADT_CUDA(cudaStreamSynchronize(P->stream));
+  if (status) std::memcpy(status, P->h_status.data(), P->ns * sizeof(adt_solve_status));
   return ADT_OK;
 }
 

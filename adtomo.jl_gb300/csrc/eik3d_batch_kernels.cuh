@@ -67,6 +67,7 @@ struct BatchArgs {
   int* meta;                // chunk brick meta: mod[nb] then proc[nb] per solve
   int64_t* seed_idx;        // chunk seeds (sorted, merged)
   T* seed_val;
+  T* gdense;                // chunk seed values as a dense field (0 off the seeds), or null
   int* n_seed;              // per chunk-local solve... indexed by global solve
   T* snap;                  // per-CTA snapshot (reference stopping rule), or null
   int64_t snap_stride;
@@ -94,10 +95,14 @@ __device__ __forceinline__ void group_sync(int grp, int nthreads) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(grp + 1), "r"(nthreads) : "memory");
 }
 
+// Brick metadata of one solve: two arrays of one int per brick, mod and proc
+// (timestamps of the last change and of the last sweep).
+constexpr int META_ARRAYS = 2;
+
 // Dynamic shared memory: [G GroupShared][G * 2 * max_nb meta ints][warp tiles]
 __host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_nb) {
   size_t b = ((size_t)G * sizeof(GroupShared) + 15) / 16 * 16;
-  if (meta_smem) b += ((size_t)G * 2 * max_nb * sizeof(int) + 15) / 16 * 16;
+  if (meta_smem) b += ((size_t)G * META_ARRAYS * max_nb * sizeof(int) + 15) / 16 * 16;
   return b;
 }
 
@@ -133,8 +138,8 @@ __device__ __forceinline__ double from_ordered<double>(unsigned long long b) {
   return __longlong_as_double((long long)b);
 }
 
-// Does brick (bx, by, bz) need a sweep at time t of its level?  It does if it
-// changed in its own last sweep, or a face neighbour changed after that.
+// Does brick b = (bx, by, bz) need a sweep at time t of its level?  It does
+// if it changed in its own last sweep, or a face neighbour changed after that.
 //
 // Every warp of the group evaluates this for the whole level while other
 // warps may already be sweeping bricks of the same level, and all must get
@@ -145,10 +150,9 @@ __device__ __forceinline__ double from_ordered<double>(unsigned long long b) {
 // words (dirty, as the sweeper found), proc == t (dirty by the first test) or
 // the old proc with mod == t (dirty by the second), so the answer is the same.
 __device__ __forceinline__ bool brick_dirty(const int* mod_, const int* proc_, const Geom& g,
-                                            int bx, int by, int bz, int t) {
+                                            int b, int bx, int by, int bz, int t) {
   const volatile int* mod = mod_;
   const volatile int* proc = proc_;
-  const int b = (bx * g.nby + by) * g.nbz + bz;
   const int pr = proc[b];
   if (pr == t) return true;
   bool v = mod[b] >= pr;
@@ -162,47 +166,12 @@ __device__ __forceinline__ bool brick_dirty(const int* mod_, const int* proc_, c
   return v;
 }
 
-// Run body(p) on this warp's share of the dirty bricks of the level
-// [q0, q1) of the level list.  Each warp forms the level's dirty mask itself
-// (one lane per brick, 32 bricks at a time) and takes the dirty bricks of
-// rank gw, gw + GW, ...: the group's warps get equal shares of the work
-// however the dirty bricks are spread over the level, without a barrier.
-template <int BK, class Body>
-__device__ __forceinline__ void for_dirty_bricks(const int* mod, const int* proc, const Geom& g,
-                                                 const uint32_t* __restrict__ bricks, int q0,
-                                                 int q1, int t, int si, int sj, int sk, int gw,
-                                                 int GW, int lane, Body&& body) {
-  int slot = 0;
-  for (int c0 = q0; c0 < q1; c0 += 32) {
-    const int qq = c0 + lane;
-    uint32_t packed = 0;
-    bool dv = false;
-    if (qq < q1) {
-      packed = bricks[qq];
-      int rx, ry, rz;
-      unpack_brick(packed, rx, ry, rz);
-      const int bx = si > 0 ? rx : g.nbx - 1 - rx;
-      const int by = sj > 0 ? ry : g.nby - 1 - ry;
-      const int bz = sk > 0 ? rz : g.nbz - 1 - rz;
-      dv = brick_dirty(mod, proc, g, bx, by, bz, t);
-    }
-    unsigned m = __ballot_sync(0xffffffffu, dv);
-    while (m) {
-      const int bit = __ffs(m) - 1;
-      m &= m - 1;
-      const uint32_t pk = __shfl_sync(0xffffffffu, packed, bit);
-      if (slot == gw) body(brick_pos<BK>(g, pk, si, sj, sk));
-      if (++slot == GW) slot = 0;
-    }
-  }
-}
-
 // ------------------------------------------------------------------ forward
 // Group layout helpers shared by the forward and adjoint kernels.
 struct GroupCtx {
   int NW, GW, G, warp, lane, grp, gw, gthreads;
   GroupShared* gs;
-  int* smeta;  // this group's meta (2 * max_nb ints) or null
+  int* smeta;  // this group's meta (META_ARRAYS * max_nb ints) or null
   unsigned char* tiles;
 };
 
@@ -219,7 +188,9 @@ __device__ __forceinline__ GroupCtx group_ctx(const BatchArgs<T>& A, unsigned ch
   c.gthreads = c.GW * 32;
   c.gs = reinterpret_cast<GroupShared*>(smem) + c.grp;
   const size_t g0 = ((size_t)c.G * sizeof(GroupShared) + 15) / 16 * 16;
-  c.smeta = A.meta_smem ? reinterpret_cast<int*>(smem + g0) + (size_t)c.grp * 2 * A.max_nb : nullptr;
+  c.smeta = A.meta_smem
+                ? reinterpret_cast<int*>(smem + g0) + (size_t)c.grp * META_ARRAYS * A.max_nb
+                : nullptr;
   c.tiles = smem + group_hdr_bytes(c.G, A.meta_smem, A.max_nb);
   return c;
 }
@@ -241,6 +212,65 @@ __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx&
     group_sync(c.grp, c.gthreads);
   }
   return q < A.n_solves ? q : -1;
+}
+
+// One ordering of one solve, level by level (bricks of level bx+by+bz in
+// the ordering's own coordinates are independent; a level's sweeps read the
+// previous level's new values and the next level's old ones -- the
+// Gauss-Seidel data flow of the reference's loop).  For each level every
+// warp of the group forms the level's dirty-brick mask itself (one lane per
+// brick, 32 bricks at a time, brick_dirty) and sweeps the dirty bricks of
+// rank gw, gw + GW, ...: equal shares however the dirty bricks are spread,
+// without a barrier before the level; one named barrier after it.
+//
+// body(p) sweeps one dirty brick and returns whether it changed; this
+// function keeps the brick's timestamps (t = ts0 + level) and counters.
+template <int BK, class Body>
+__device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, const uint32_t* bricks,
+                                             const int* lstart, int* mod, int* proc, int ts0,
+                                             int si, int sj, int sk,
+                                             unsigned long long& cnt_upd,
+                                             unsigned long long& cnt_brk, Body&& body) {
+  const int lane = c.lane;
+  for (int d = 0; d < g.nlev; ++d) {
+    const int t = ts0 + d;
+    const int q0 = lstart[d], q1 = lstart[d + 1];
+    int slot = 0;
+    for (int c0 = q0; c0 < q1; c0 += 32) {
+      const int qq = c0 + lane;
+      uint32_t packed = 0;
+      bool dv = false;
+      if (qq < q1) {
+        packed = bricks[qq];
+        int rx, ry, rz;
+        unpack_brick(packed, rx, ry, rz);
+        const int bx = si > 0 ? rx : g.nbx - 1 - rx;
+        const int by = sj > 0 ? ry : g.nby - 1 - ry;
+        const int bz = sk > 0 ? rz : g.nbz - 1 - rz;
+        dv = brick_dirty(mod, proc, g, (bx * g.nby + by) * g.nbz + bz, bx, by, bz, t);
+      }
+      unsigned m = __ballot_sync(0xffffffffu, dv);
+      while (m) {
+        const int bit = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t pk = __shfl_sync(0xffffffffu, packed, bit);
+        if (slot == c.gw) {
+          const BrickPos p = brick_pos<BK>(g, pk, si, sj, sk);
+          const bool ch = body(p);
+          __syncwarp();
+          if (lane == 0) {
+            const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
+            proc[b] = t;
+            if (ch) mod[b] = t;
+            cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
+            cnt_brk += 1;
+          }
+        }
+        if (++slot == c.GW) slot = 0;
+      }
+    }
+    group_sync(c.grp, c.gthreads);
+  }
 }
 
 // Select the sweep instantiation for the ordering's directions and the
@@ -338,28 +368,17 @@ __global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
         int si, sj, sk;
         ordering3(o, si, sj, sk);
         const int CS = tile_col_stride(BK, sj == sk);
-        for (int d = 0; d < g.nlev; ++d) {
-          const int t = (it * 8 + o) * g.nlev + d;
-          for_dirty_bricks<BK>(mod, proc, g, fd.bricks, fd.lstart[d], fd.lstart[d + 1], t, si, sj,
-                               sk, c.gw, c.GW, lane, [&](const BrickPos& p) {
-            bool ch;
-            if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
-              if (vec) {
-                load_tile_f32_vec<BK>(S, u, g, p, CS, lane);
-                load_interior_f32_vec<BK>(F, fd.f, g, p, CS, lane);
-                __syncwarp();
-                const bool nr = use_near && box.hits(p);
-                ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, md);
-                if (ch) store_interior_f32_vec<BK>(S, u, g, p, CS, lane);
-              } else {
-                load_halo_tile<T, BK>(S, u, g, p, CS, lane);
-                load_interior<T, BK>(F, fd.f, g, p, CS, lane);
-                cp_async_wait_all();
-                __syncwarp();
-                ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
-                                                  use_near && box.hits(p), lane, md);
-                if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
-              }
+        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, (it * 8 + o) * g.nlev, si, sj, sk,
+                         cnt_upd, cnt_brk, [&](const BrickPos& p) -> bool {
+          bool ch;
+          if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
+            if (vec) {
+              load_tile_f32_vec<BK>(S, u, g, p, CS, lane);
+              load_interior_f32_vec<BK>(F, fd.f, g, p, CS, lane);
+              __syncwarp();
+              const bool nr = use_near && box.hits(p);
+              ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, md);
+              if (ch) store_interior_f32_vec<BK>(S, u, g, p, CS, lane);
             } else {
               load_halo_tile<T, BK>(S, u, g, p, CS, lane);
               load_interior<T, BK>(F, fd.f, g, p, CS, lane);
@@ -369,17 +388,17 @@ __global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
                                                 use_near && box.hits(p), lane, md);
               if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
             }
+          } else {
+            load_halo_tile<T, BK>(S, u, g, p, CS, lane);
+            load_interior<T, BK>(F, fd.f, g, p, CS, lane);
+            cp_async_wait_all();
             __syncwarp();
-            if (lane == 0) {
-              const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
-              proc[b] = t;
-              if (ch) mod[b] = t;
-              cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
-              cnt_brk += 1;
-            }
-          });
-          group_sync(c.grp, c.gthreads);
-        }
+            ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
+                                              use_near && box.hits(p), lane, md);
+            if (ch) store_interior<T, BK>(S, u, g, p, CS, lane);
+          }
+          return ch;
+        });
       }
       if (snap) {
         T mx = T(0);
@@ -534,6 +553,7 @@ __global__ void k_batch_misfit(BatchArgs<T> A, const double* __restrict__ t_obs,
         if (cur >= 0) {
           sidx[ns] = cur;
           sval[ns] = (T)acc;
+          if (A.gdense) A.gdense[sd.u_off + cur] = (T)acc;
           ++ns;
         }
         cur = cell;
@@ -544,6 +564,7 @@ __global__ void k_batch_misfit(BatchArgs<T> A, const double* __restrict__ t_obs,
     if (cur >= 0) {
       sidx[ns] = cur;
       sval[ns] = (T)acc;
+      if (A.gdense) A.gdense[sd.u_off + cur] = (T)acc;
       ++ns;
     }
     A.n_seed[sd.gidx] = ns;
@@ -577,18 +598,18 @@ __device__ __forceinline__ int upwind_side_t(const T* u, int64_t c, int pos, int
 
 template <int BK>
 __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const uint16_t* C,
-                                                 const int64_t* sidx, const float* sval,
-                                                 int ns, const Geom& g, const BrickPos& p, int si,
-                                                 int sj, int sk, int lane) {
+                                                 const float* gcell, const Geom& g,
+                                                 const BrickPos& p, int si, int sj, int sk,
+                                                 int lane) {
   switch ((si < 0) | ((sj < 0) << 1) | ((sk < 0) << 2)) {
-    case 0: return sweep_brick_adj_f32<BK, 1, 1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
-    case 1: return sweep_brick_adj_f32<BK, -1, 1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
-    case 2: return sweep_brick_adj_f32<BK, 1, -1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
-    case 3: return sweep_brick_adj_f32<BK, -1, -1, 1>(U, L, C, sidx, sval, ns, g, p, lane);
-    case 4: return sweep_brick_adj_f32<BK, 1, 1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
-    case 5: return sweep_brick_adj_f32<BK, -1, 1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
-    case 6: return sweep_brick_adj_f32<BK, 1, -1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
-    default: return sweep_brick_adj_f32<BK, -1, -1, -1>(U, L, C, sidx, sval, ns, g, p, lane);
+    case 0: return sweep_brick_adj_f32<BK, 1, 1, 1>(U, L, C, gcell, g, p, lane);
+    case 1: return sweep_brick_adj_f32<BK, -1, 1, 1>(U, L, C, gcell, g, p, lane);
+    case 2: return sweep_brick_adj_f32<BK, 1, -1, 1>(U, L, C, gcell, g, p, lane);
+    case 3: return sweep_brick_adj_f32<BK, -1, -1, 1>(U, L, C, gcell, g, p, lane);
+    case 4: return sweep_brick_adj_f32<BK, 1, 1, -1>(U, L, C, gcell, g, p, lane);
+    case 5: return sweep_brick_adj_f32<BK, -1, 1, -1>(U, L, C, gcell, g, p, lane);
+    case 6: return sweep_brick_adj_f32<BK, 1, -1, -1>(U, L, C, gcell, g, p, lane);
+    default: return sweep_brick_adj_f32<BK, -1, -1, -1>(U, L, C, gcell, g, p, lane);
   }
 }
 
@@ -685,29 +706,17 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
         int si, sj, sk;
         ordering3(o, si, sj, sk);
         const int CS = tile_col_stride(BK, sj == sk);
-        for (int d = 0; d < g.nlev; ++d) {
-          const int t = (it * 8 + o) * g.nlev + d;
-          for_dirty_bricks<BK>(mod, proc, g, fd.bricks, fd.lstart[d], fd.lstart[d + 1], t, si, sj,
-                               sk, c.gw, c.GW, lane, [&](const BrickPos& p) {
-            bool ch;
-            if constexpr (sizeof(T) == 4) {
-              if (vec) {
-                load_tile_f32_vec<BK>(U, u, g, p, CS, lane);
-                load_tile_f32_vec<BK>(L, lam, g, p, CS, lane, 0.0f);
-                load_codes_vec<BK>(C, code, g, p, CS, lane);
-                __syncwarp();
-                ch = dispatch_adj_f32<BK>(U, L, C, sidx, sval, ns, g, p, si, sj, sk, lane);
-                if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
-              } else {
-                load_halo_tile<T, BK>(U, u, g, p, CS, lane);
-                load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
-                load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
-                cp_async_wait_all();
-                __syncwarp();
-                ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si,
-                                                          sj, sk, CS, lane);
-                if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
-              }
+        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, (it * 8 + o) * g.nlev, si, sj, sk,
+                         cnt_upd, cnt_brk, [&](const BrickPos& p) -> bool {
+          bool ch;
+          if constexpr (sizeof(T) == 4) {
+            if (vec) {
+              load_tile_f32_vec<BK>(U, u, g, p, CS, lane);
+              load_tile_f32_vec<BK>(L, lam, g, p, CS, lane, 0.0f);
+              load_codes_vec<BK>(C, code, g, p, CS, lane);
+              __syncwarp();
+              ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane);
+              if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
             } else {
               load_halo_tile<T, BK>(U, u, g, p, CS, lane);
               load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
@@ -718,18 +727,19 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
                                                         sj, sk, CS, lane);
               if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
             }
+          } else {
+            load_halo_tile<T, BK>(U, u, g, p, CS, lane);
+            load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
+            load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
+            cp_async_wait_all();
             __syncwarp();
-            if (lane == 0) {
-              const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
-              proc[b] = t;
-              if (ch) mod[b] = t;
-              cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
-              cnt_brk += 1;
-            }
-            any |= ch;
-          });
-          group_sync(c.grp, c.gthreads);
-        }
+            ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si,
+                                                      sj, sk, CS, lane);
+            if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+          }
+          any |= ch;
+          return ch;
+        });
       }
       if (any && lane == 0) c.gs->changed = 1;
       group_sync(c.grp, c.gthreads);
@@ -740,6 +750,8 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
         break;
       }
     }
+    if (A.gdense)  // leave the dense seed field all zero for the next evaluation
+      for (int e = c.gw * 32 + lane; e < ns; e += c.gthreads) A.gdense[sd.u_off + sidx[e]] = T(0);
     if (c.gw == 0 && lane == 0) {
       adt_solve_status& st = A.status[sd.gidx];
       st.adj_iters = conv ? it + 1 : it;

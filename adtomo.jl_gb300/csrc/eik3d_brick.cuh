@@ -201,7 +201,10 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
 
 // ---------------------------------------------------------------------------
 // FP32 staging with 16-byte vector loads (grids whose k extent is a multiple
-// of 4, so every brick column segment starts on a 16-byte boundary).  The 56
+// of 4, so every brick column segment starts on a 16-byte boundary).  Travel
+// times, adjoint variables and codes are written during the kernel by other
+// warps, so they are read with ordinary (coherent) loads; only the slowness
+// goes through the read-only path.  The 56
 // columns of a halo tile (32 interior, 24 face columns) are split into
 // 4-float chunks; lane t takes chunks t, t+32, ...  Out-of-grid cells of the
 // halo are written as `ghost`: +inf for travel times, so min(neighbour pair)
@@ -230,7 +233,7 @@ __device__ __forceinline__ void halo_col(int c, int& ci, int& cj) {
 constexpr int LOAD_BATCH = 7;
 
 template <int BK>
-__device__ __forceinline__ void load_tile_f32_vec(float* S, const float* __restrict__ src,
+__device__ __forceinline__ void load_tile_f32_vec(float* S, const float* src,
                                                   const Geom& g, const BrickPos& p, int CS,
                                                   int lane,
                                                   float ghost = INFINITY) {
@@ -247,8 +250,8 @@ __device__ __forceinline__ void load_tile_f32_vec(float* S, const float* __restr
     const int i = p.i0 + hci - 1, j = p.j0 + hcj - 1;
     if (i < g.m && j < g.n) {
       const float* col = src + ((int64_t)i * g.n + j) * g.l + p.k0;
-      if (p.k0 > 0) hlo = __ldg(col - 1);
-      if (p.k0 + p.nk < g.l) hhi = __ldg(col + p.nk);
+      if (p.k0 > 0) hlo = col[-1];
+      if (p.k0 + p.nk < g.l) hhi = col[p.nk];
     }
   }
 #pragma unroll
@@ -264,7 +267,7 @@ __device__ __forceinline__ void load_tile_f32_vec(float* S, const float* __restr
       const int i = p.i0 + ci - 1, j = p.j0 + cj - 1, k = 4 * ch;
       v[t] = make_float4(INF, INF, INF, INF);
       if (i >= 0 && i < g.m && j >= 0 && j < g.n && k < p.nk)
-        v[t] = __ldg(reinterpret_cast<const float4*>(src + ((int64_t)i * g.n + j) * g.l + p.k0 + k));
+        v[t] = *reinterpret_cast<const float4*>(src + ((int64_t)i * g.n + j) * g.l + p.k0 + k);
       dst[t] = ci * RS + cj * CS + 1 + k;
     }
 #pragma unroll
@@ -456,7 +459,7 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
 // Interior codes (uint16) with 16-byte vector loads: 8 codes per chunk.
 // Needs the k extent to be a multiple of 8 (16-byte aligned column segments).
 template <int BK>
-__device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* __restrict__ src,
+__device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* src,
                                                const Geom& g, const BrickPos& p, int CS, int lane) {
   constexpr int IRS = itile_row_stride(BK);
   constexpr int CH = BK / 8;
@@ -471,7 +474,7 @@ __device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* __re
     const int ci = c >> 2, cj = c & 3, k = 8 * ch;
     ok[t] = ci < p.ni && cj < p.nj && k < p.nk;
     if (ok[t])
-      v[t] = __ldg(reinterpret_cast<const uint4*>(
+      v[t] = *(reinterpret_cast<const uint4*>(
           src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k));
     dst[t] = ci * IRS + cj * CS + k;
   }
@@ -532,8 +535,7 @@ template <int SI, int SJ, int SKD>
 __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, float uxu, float uxd,
                                                    float uyu, float uyd, float uzu, float uzd,
                                                    float lxd, float lyd, float lzd, bool act,
-                                                   int64_t key, const int64_t* seed_idx,
-                                                   const float* seed_val, int n_seed) {
+                                                   int64_t cell, const float* gcell) {
   // user bits (absolute: x-, x+, y-, y+, z-, z+) and upwind side codes
   // (1 minus, 2 plus) of the upstream / downstream neighbours of this sweep
   constexpr uint32_t XU = SI > 0 ? 1u : 2u, XD = SI > 0 ? 2u : 1u;
@@ -555,15 +557,7 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
   float d = sx ? uc - (sx == SXU ? uxu : uxd) : 0.0f;
   d += sy ? uc - (sy == SYU ? uyu : uyd) : 0.0f;
   d += sz ? uc - (sz == SZU ? uzu : uzd) : 0.0f;
-  float gs = 0.0f;
-  if (act && (code & CODE_SEED)) {
-    int lo = 0, hi = n_seed - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (seed_idx[mid] < key) lo = mid + 1; else hi = mid;
-    }
-    gs = seed_val[lo];
-  }
+  const float gs = (act && (code & CODE_SEED)) ? gcell[cell] : 0.0f;
   c.c2 = rcp_approx(d);
   c.c0 = 0.5f * gs * c.c2;
   c.wrok = act && !(code & CODE_FIXED);
@@ -580,9 +574,8 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
 // share one tile layout; SI, SJ, SKD: sweep directions.
 template <int BK, int SI, int SJ, int SKD>
 __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, const uint16_t* C,
-                                                    const int64_t* seed_idx, const float* seed_val,
-                                                    int n_seed, const Geom& g, const BrickPos& p,
-                                                    int lane) {
+                                                    const float* gcell, const Geom& g,
+                                                    const BrickPos& p, int lane) {
   constexpr int RS = tile_row_stride(BK);
   constexpr int IRS = itile_row_stride(BK);
   constexpr int CS = tile_col_stride(BK, SJ == SKD);
@@ -607,8 +600,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
   float lzu = lds<-DZ>(la);
   AdjCellF32 cur = adj_cell_f32<SI, SJ, SKD>(
       ldsu16(ca), uc, lds<XU>(ua), lds<XD>(ua), lds<YU>(ua), lds<YD>(ua), lds<-DZ>(ua), uzd,
-      lds<XD>(la), lds<YD>(la), lzd, (unsigned)(-s) < (unsigned)nk, gcol - SKD * s, seed_idx,
-      seed_val, n_seed);
+      lds<XD>(la), lds<YD>(la), lzd, (unsigned)(-s) < (unsigned)nk, gcol - SKD * s, gcell);
   bool changed = false;
   const int nsteps = p.nk + SKEW;
 #pragma unroll 1
@@ -632,7 +624,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
     const int kn = tau + 1 - s;
     cur = adj_cell_f32<SI, SJ, SKD>(n_code, uzd, n_uxu, n_uxd, n_uyu, n_uyd, uc, n_uzd, n_lxd,
                                     n_lyd, n_lzd, (unsigned)kn < (unsigned)nk, gcol + SKD * kn,
-                                    seed_idx, seed_val, n_seed);
+                                    gcell);
     uc = uzd;
     uzd = n_uzd;
     lold = lzd;
