@@ -358,11 +358,13 @@ __device__ __forceinline__ float upd3_f32(float ax, float ay, float az, float fh
   const float F2 = fh * fh;
   const float d2 = mid - lo;
   const float d3 = hi - lo;
-  const float e = d3 - d2;
   const float x1 = lo + fh;
   const float r2 = sqrt_approx(fmaxf(fmaf(-d2, d2, 2.0f * F2), 0.0f));
   const float x2 = fmaf(0.5f, d2 + r2, lo);
-  const float r3 = sqrt_approx(fmaxf(3.0f * F2 - d2 * d2 - d3 * d3 - e * e, 0.0f));
+  // 3F^2 - d2^2 - d3^2 - (d3 - d2)^2 = 3F^2 - 2 (d2 (d2 - d3) + d3^2): two
+  // dependent operations fewer than the sum of three squares
+  const float q = fmaf(d2, d2 - d3, d3 * d3);
+  const float r3 = sqrt_approx(fmaxf(fmaf(-2.0f, q, 3.0f * F2), 0.0f));
   const float x3 = fmaf(d2 + d3 + r3, 1.0f / 3.0f, lo);
   return (x1 <= mid) ? x1 : ((x2 <= hi) ? x2 : x3);
 }
@@ -423,7 +425,7 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
   float fc = lds<0>(fa);
   float mb = 0.0f;
   const int nsteps = p.nk + SKEW;
-#pragma unroll 1
+#pragma unroll 4
   for (int tau = 0; tau < nsteps; ++tau) {
     const int kk = tau - s;
     const bool act = (unsigned)kk < (unsigned)nk;
@@ -603,7 +605,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
       lds<XD>(la), lds<YD>(la), lzd, (unsigned)(-s) < (unsigned)nk, gcol - SKD * s, gcell);
   bool changed = false;
   const int nsteps = p.nk + SKEW;
-#pragma unroll 1
+#pragma unroll 4
   for (int tau = 0; tau < nsteps; ++tau) {
     const float lxu = lds<XU>(la), lyu = lds<YU>(la);
     // next cell's operands
