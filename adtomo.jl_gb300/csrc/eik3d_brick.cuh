@@ -538,12 +538,11 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
                                                    float uyu, float uyd, float uzu, float uzd,
                                                    float lxd, float lyd, float lzd, bool act,
                                                    int64_t cell, const float* gcell) {
-  // user bits (absolute: x-, x+, y-, y+, z-, z+) and upwind side codes
-  // (1 minus, 2 plus) of the upstream / downstream neighbours of this sweep
+  // user bits (absolute: x-, x+, y-, y+, z-, z+) of the upstream /
+  // downstream neighbours of this sweep
   constexpr uint32_t XU = SI > 0 ? 1u : 2u, XD = SI > 0 ? 2u : 1u;
   constexpr uint32_t YU = SJ > 0 ? 4u : 8u, YD = SJ > 0 ? 8u : 4u;
   constexpr uint32_t ZU = SKD > 0 ? 16u : 32u, ZD = SKD > 0 ? 32u : 16u;
-  constexpr uint32_t SXU = SI > 0 ? 1u : 2u, SYU = SJ > 0 ? 1u : 2u, SZU = SKD > 0 ? 1u : 2u;
   const uint32_t us = code >> CODE_USERS;
   AdjCellF32 c;
   c.wx = (us & XU) ? uxu - uc : 0.0f;
@@ -555,10 +554,12 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
   if (SI > 0) { c.ax = w_xd; c.bx = lxd; } else { c.ax = w_xd * lxd; c.bx = 0.0f; }
   if (SJ > 0) { c.ay = w_yd; c.by = lyd; } else { c.ay = w_yd * lyd; c.by = 0.0f; }
   if (SKD > 0) { c.az = w_zd; c.bz = lzd; } else { c.az = w_zd * lzd; c.bz = 0.0f; }
-  const uint32_t sx = code & 3u, sy = (code >> 2) & 3u, sz = (code >> 4) & 3u;
-  float d = sx ? uc - (sx == SXU ? uxu : uxd) : 0.0f;
-  d += sy ? uc - (sy == SYU ? uyu : uyd) : 0.0f;
-  d += sz ? uc - (sz == SZU ? uzu : uzd) : 0.0f;
+  // The diagonal needs no side codes: an axis is active exactly when u_c
+  // exceeds the smaller neighbour, which is the upwind one (the codes' tie
+  // rule picks between equal values), and out-of-grid ghosts are +inf.
+  float d = fmaxf(uc - fminf(uxu, uxd), 0.0f);
+  d += fmaxf(uc - fminf(uyu, uyd), 0.0f);
+  d += fmaxf(uc - fminf(uzu, uzd), 0.0f);
   const float gs = (act && (code & CODE_SEED)) ? gcell[cell] : 0.0f;
   c.c2 = rcp_approx(d);
   c.c0 = 0.5f * gs * c.c2;
