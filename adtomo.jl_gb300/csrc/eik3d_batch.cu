@@ -115,6 +115,8 @@ struct BatchPlan {
   std::vector<double> h;
   std::vector<int> nsta;
   std::vector<int64_t> cell_off, sta_off;
+  std::vector<int64_t> cell_off_t;  // FP32 slowness copy: per-field offsets padded to 16 cells
+  int64_t ncell_t_total = 0;
   int64_t ncell_total = 0;
   // solves
   int ns = 0;
@@ -216,8 +218,10 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     P->h.push_back(hh[f]);
     P->nsta.push_back(nsta[f]);
     P->cell_off.push_back(P->ncell_total);
+    P->cell_off_t.push_back(P->ncell_t_total);
     P->sta_off.push_back(sofs);
     P->ncell_total += g.ncell;
+    P->ncell_t_total += (g.ncell + 15) / 16 * 16;
     for (int q = 0; q < nsta[f]; ++q) {
       const double* x = sta_xyz + 3 * (sofs + q);
       if (!(x[0] >= 0 && x[0] <= g.m - 1 && x[1] >= 0 && x[1] <= g.n - 1 && x[2] >= 0 && x[2] <= g.l - 1))
@@ -275,7 +279,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       P->solves[s].meta_off = bricks;
       P->solves[s].seed_off = seeds;
       ch.field_uoff[P->solve_field[s]].push_back(cells);
-      cells += g.ncell;
+      cells += (g.ncell + 15) / 16 * 16;  // 64-byte aligned solves: the FP32 path uses 16-byte accesses
       bricks += (int64_t)META_ARRAYS * g.nbx * g.nby * g.nbz;
       seeds += 8LL * P->nsta[P->solve_field[s]];
     }
@@ -304,7 +308,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   if ((rc = R(b, n))) return rc;
   R_(P->d_slow64, P->ncell_total * 8);
   R_(P->d_slow0, P->ncell_total * 8);
-  R_(P->d_slowT, P->f64 ? 16 : P->ncell_total * 4);
+  R_(P->d_slowT, P->f64 ? 16 : P->ncell_t_total * 4);
   R_(P->d_sta, (size_t)sofs * 3 * 8);
   R_(P->d_tobs, P->nobs * 8);
   R_(P->d_w, P->nobs * 8);
@@ -369,7 +373,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].h = P->h[f];
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
       fdv[f].f0 = P->d_slow0.as<double>() + P->cell_off[f];
-      fdv[f].f = P->d_slowT.as<float>() + P->cell_off[f];
+      fdv[f].f = P->d_slowT.as<float>() + P->cell_off_t[f];  // 64-byte aligned (16-byte loads)
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
       fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
@@ -501,8 +505,10 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
   // inside a graph capture the timing events must be external event nodes
   const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (!P.f64)
-    k_to_t_f32<<<grid1d(P.ncell_total), 256, 0, st>>>(P.d_slow64.as<double>(), P.d_slowT.as<float>(),
-                                                      P.ncell_total);
+    for (int f = 0; f < P.nf; ++f)
+      k_to_t_f32<<<grid1d(P.geoms[f].ncell), 256, 0, st>>>(P.d_slow64.as<double>() + P.cell_off[f],
+                                                           P.d_slowT.as<float>() + P.cell_off_t[f],
+                                                           P.geoms[f].ncell);
   k_src_init<T><<<(P.ns + 127) / 128, 128, 0, st>>>(P.d_solves.as<SolveDev>(), P.ns,
                                                      P.d_fields.as<FieldDev<T>>(),
                                                      P.src_fixed ? 1 : 0);

@@ -596,6 +596,85 @@ __device__ __forceinline__ int upwind_side_t(const T* u, int64_t c, int pos, int
   return (uc > a) ? side : 0;
 }
 
+// Codes of four consecutive cells of one column (FP32, l % 4 == 0), from
+// 16-byte loads: the same rule as upwind_side_t and the fixed-cell test,
+// with out-of-grid neighbours read as +inf (so the edge cases fall out of the
+// comparisons).  Writes the four codes (one 8-byte store) and lambda = 0.
+__device__ __forceinline__ void adj_pass1_vec4(const float* u, uint16_t* code, float* lam,
+                                               const SolveDev& sd, const Geom& g, int64_t x,
+                                               int i, int j, int k) {
+  const float INF = __int_as_float(0x7f800000);
+  const float4 INF4 = make_float4(INF, INF, INF, INF);
+  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+  const float4 c4 = *reinterpret_cast<const float4*>(u + x);
+  const float4 xm = i > 0 ? *reinterpret_cast<const float4*>(u + x - sI) : INF4;
+  const float4 xp = i < g.m - 1 ? *reinterpret_cast<const float4*>(u + x + sI) : INF4;
+  const float4 ym = j > 0 ? *reinterpret_cast<const float4*>(u + x - sJ) : INF4;
+  const float4 yp = j < g.n - 1 ? *reinterpret_cast<const float4*>(u + x + sJ) : INF4;
+  const float zm = k > 0 ? u[x - 1] : INF;
+  const float zp = k + 4 < g.l ? u[x + 4] : INF;
+  const float uc[4] = {c4.x, c4.y, c4.z, c4.w};
+  const float vxm[4] = {xm.x, xm.y, xm.z, xm.w}, vxp[4] = {xp.x, xp.y, xp.z, xp.w};
+  const float vym[4] = {ym.x, ym.y, ym.z, ym.w}, vyp[4] = {yp.x, yp.y, yp.z, yp.w};
+  uint32_t packed[2] = {0u, 0u};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float um[3] = {vxm[q], vym[q], q == 0 ? zm : uc[q - 1]};
+    const float up[3] = {vxp[q], vyp[q], q == 3 ? zp : uc[q + 1]};
+    uint32_t cd = 0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {  // upwind side: the smaller neighbour, ties to +1
+      const bool minus = up[ax] > um[ax];
+      const float a = minus ? um[ax] : up[ax];
+      cd |= (uc[q] > a ? (minus ? 1u : 2u) : 0u) << (2 * ax);
+    }
+    if (uc[q] == (float)u0_at(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
+    packed[q >> 1] |= cd << (16 * (q & 1));
+  }
+  *reinterpret_cast<uint2*>(code + x) = make_uint2(packed[0], packed[1]);
+  *reinterpret_cast<float4*>(lam + x) = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// User bits of four consecutive cells (pass 2) from 8-byte loads of the
+// codes: neighbour r uses c when r is not fixed and its upwind side along
+// the axis points at c.
+__device__ __forceinline__ void adj_pass2_vec4(uint16_t* code, const Geom& g, int64_t x, int i,
+                                               int j, int k) {
+  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+  auto ld4 = [&](int64_t y) -> uint2 { return *reinterpret_cast<const uint2*>(code + y); };
+  auto c16 = [](uint2 v, int q) -> uint32_t {
+    return ((q < 2 ? v.x : v.y) >> (16 * (q & 1))) & 0xffffu;
+  };
+  const uint2 zero = make_uint2(CODE_FIXED | (CODE_FIXED << 16), CODE_FIXED | (CODE_FIXED << 16));
+  const uint2 c4 = ld4(x);
+  const uint2 xm = i > 0 ? ld4(x - sI) : zero;
+  const uint2 xp = i < g.m - 1 ? ld4(x + sI) : zero;
+  const uint2 ym = j > 0 ? ld4(x - sJ) : zero;
+  const uint2 yp = j < g.n - 1 ? ld4(x + sJ) : zero;
+  const uint32_t zm = k > 0 ? (uint32_t)code[x - 1] : CODE_FIXED;
+  const uint32_t zp = k + 4 < g.l ? (uint32_t)code[x + 4] : CODE_FIXED;
+  auto uses = [](uint32_t cr, int ax, uint32_t want) -> bool {
+    return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
+  };
+  uint32_t packed[2] = {0u, 0u};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t cd = c16(c4, q);
+    if (!(cd & CODE_FIXED)) {
+      uint32_t us = 0;
+      if (uses(c16(xm, q), 0, 2u)) us |= 1u;
+      if (uses(c16(xp, q), 0, 1u)) us |= 2u;
+      if (uses(c16(ym, q), 1, 2u)) us |= 4u;
+      if (uses(c16(yp, q), 1, 1u)) us |= 8u;
+      if (uses(q == 0 ? zm : c16(c4, q - 1), 2, 2u)) us |= 16u;
+      if (uses(q == 3 ? zp : c16(c4, q + 1), 2, 1u)) us |= 32u;
+      cd |= us << CODE_USERS;
+    }
+    packed[q >> 1] |= cd << (16 * (q & 1));
+  }
+  *reinterpret_cast<uint2*>(code + x) = make_uint2(packed[0], packed[1]);
+}
+
 template <int BK>
 __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const uint16_t* C,
                                                  const float* gcell, const Geom& g,
@@ -642,7 +721,16 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
     const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
     const bool vec = (g.l % 8) == 0;
     // pass 1: upwind sides and fixed cells; lambda = 0
-    for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
+    const bool vec4 = sizeof(T) == 4 && (g.l % 4) == 0;
+    if constexpr (sizeof(T) == 4) {
+      if (vec4)
+        for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += c.gthreads) {
+          const int64_t col = e / (g.l / 4);
+          adj_pass1_vec4(u, code, lam, sd, g, 4 * e, (int)(col / g.n), (int)(col % g.n),
+                         (int)(4 * e - col * g.l));
+        }
+    }
+    for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
       for (int k = lane; k < g.l; k += 32) {
         const int64_t x = col * g.l + k;
@@ -662,7 +750,15 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
     }
     group_sync(c.grp, c.gthreads);
     // pass 2: users (reads only the low bits of neighbours, writes own high bits)
-    for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
+    if constexpr (sizeof(T) == 4) {
+      if (vec4)
+        for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += c.gthreads) {
+          const int64_t col = e / (g.l / 4);
+          adj_pass2_vec4(code, g, 4 * e, (int)(col / g.n), (int)(col % g.n),
+                         (int)(4 * e - col * g.l));
+        }
+    }
+    for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
       for (int k = lane; k < g.l; k += 32) {
         const int64_t x = col * g.l + k;

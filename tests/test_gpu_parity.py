@@ -315,3 +315,22 @@ def test_batch_c4_multi_field_uneven_grids():
         assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
     assert all(s.converged and s.adj_converged for s in st)
     B.close()
+
+
+def test_batch_fp32_mixed_fields_alignment():
+    """A field whose cell count is not a multiple of 4 ahead of a field that
+    takes the 16-byte-access FP32 path: every solve's buffers must still start
+    aligned (results against the FP64 oracle)."""
+    rng = np.random.default_rng(12)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(9, 7, 13, 0.5), (16, 12, 20, 0.5), (11, 9, 7, 0.5), (12, 16, 24, 0.5)], 8, 6)
+    assert fields[0][0] * fields[0][1] * fields[0][2] % 4 != 0
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4
+    for g, r in zip(grads, go):
+        assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
+    assert all(s.converged and s.adj_converged for s in st)
+    B.close()
