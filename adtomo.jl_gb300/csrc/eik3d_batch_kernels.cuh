@@ -373,8 +373,9 @@ __global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
           bool ch;
           if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
             if (vec) {
-              load_tile_f32_vec<BK>(S, u, g, p, CS, lane);
-              load_interior_f32_vec<BK>(F, fd.f, g, p, CS, lane);
+              load_tile_f32_async<BK>(S, u, g, p, CS, lane);
+              load_interior_f32_async<BK>(F, fd.f, g, p, CS, lane);
+              cp_async_wait_all();
               __syncwarp();
               const bool nr = use_near && box.hits(p);
               ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, md);
@@ -807,9 +808,10 @@ __global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
           bool ch;
           if constexpr (sizeof(T) == 4) {
             if (vec) {
-              load_tile_f32_vec<BK>(U, u, g, p, CS, lane);
-              load_tile_f32_vec<BK>(L, lam, g, p, CS, lane, 0.0f);
+              load_tile_f32_async<BK>(U, u, g, p, CS, lane);
+              load_tile_f32_async<BK>(L, lam, g, p, CS, lane, 0.0f);
               load_codes_vec<BK>(C, code, g, p, CS, lane);
+              cp_async_wait_all();
               __syncwarp();
               ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane);
               if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);

@@ -341,6 +341,84 @@ __device__ __forceinline__ void store_interior_f32_vec(const float* S, float* __
   }
 }
 
+// Asynchronous staging (cp.async, 4 bytes per copy): every element of a tile
+// is requested before any is waited for, so a brick pays the load latency
+// once instead of once per batch of register loads.  The padded tile layout
+// (odd column stride) rules out 16-byte copies; out-of-grid ghosts are plain
+// shared stores.  The caller waits with cp_async_wait_all() + __syncwarp().
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void sts4(uint32_t dst, float v) {
+  asm volatile("st.shared.f32 [%0], %1;\n" ::"r"(dst), "f"(v) : "memory");
+}
+
+template <int BK>
+__device__ __forceinline__ void load_tile_f32_async(float* S, const float* src, const Geom& g,
+                                                    const BrickPos& p, int CS, int lane,
+                                                    float ghost = INFINITY) {
+  constexpr int RS = tile_row_stride(BK);
+  constexpr int CH = BK / 4;
+  constexpr int NCOL = BI * BJ + 2 * BI + 2 * BJ;  // 56
+  constexpr int PER = NCOL * CH / 32;              // chunks per lane (exact)
+  static_assert(NCOL * CH % 32 == 0, "tile chunking");
+  const uint32_t s0 = smem_u32(S);
+  {  // k halo of the interior columns (lane c takes interior column c)
+    const int hci = (lane >> 2) + 1, hcj = (lane & 3) + 1;
+    const int i = p.i0 + hci - 1, j = p.j0 + hcj - 1;
+    const uint32_t d = s0 + 4u * (uint32_t)(hci * RS + hcj * CS);
+    const bool in = i < g.m && j < g.n;
+    const float* col = in ? src + ((int64_t)i * g.n + j) * g.l + p.k0 : src;
+    if (in && p.k0 > 0) cp_async4(d, col - 1); else sts4(d, ghost);
+    const uint32_t dh = d + 4u * (uint32_t)(1 + p.nk);
+    if (in && p.k0 + p.nk < g.l) cp_async4(dh, col + p.nk); else sts4(dh, ghost);
+  }
+#pragma unroll
+  for (int t = 0; t < PER; ++t) {
+    const int e = lane + 32 * t;
+    const int c = e / CH, ch = e - (e / CH) * CH;
+    int ci, cj;
+    halo_col(c, ci, cj);
+    const int i = p.i0 + ci - 1, j = p.j0 + cj - 1, k = 4 * ch;
+    const uint32_t d = s0 + 4u * (uint32_t)(ci * RS + cj * CS + 1 + k);
+    if (i >= 0 && i < g.m && j >= 0 && j < g.n && k < p.nk) {
+      const float* sp = src + ((int64_t)i * g.n + j) * g.l + p.k0 + k;
+      cp_async4(d, sp);
+      cp_async4(d + 4, sp + 1);
+      cp_async4(d + 8, sp + 2);
+      cp_async4(d + 12, sp + 3);
+    } else {
+      sts4(d, ghost);
+      sts4(d + 4, ghost);
+      sts4(d + 8, ghost);
+      sts4(d + 12, ghost);
+    }
+  }
+}
+
+template <int BK>
+__device__ __forceinline__ void load_interior_f32_async(float* S, const float* src, const Geom& g,
+                                                        const BrickPos& p, int CS, int lane) {
+  constexpr int IRS = itile_row_stride(BK);
+  constexpr int CH = BK / 4;
+  constexpr int PER = BI * BJ * CH / 32;
+  const uint32_t s0 = smem_u32(S);
+#pragma unroll
+  for (int t = 0; t < PER; ++t) {
+    const int e = lane + 32 * t;
+    const int c = e / CH, ch = e - (e / CH) * CH;
+    const int ci = c >> 2, cj = c & 3, k = 4 * ch;
+    if (ci < p.ni && cj < p.nj && k < p.nk) {
+      const float* sp = src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k;
+      const uint32_t d = s0 + 4u * (uint32_t)(ci * IRS + cj * CS + k);
+      cp_async4(d, sp);
+      cp_async4(d + 4, sp + 1);
+      cp_async4(d + 8, sp + 2);
+      cp_async4(d + 12, sp + 3);
+    }
+  }
+}
+
 // Hardware square root (MUFU, ~1 ulp), for the FP32 path only.
 __device__ __forceinline__ float sqrt_approx(float x) {
   float r;
