@@ -406,8 +406,9 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   cudaFuncAttributes fa_f, fa_a;
   ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
   ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
-  auto shape = [&](size_t warp_bytes, int gw_default, int regs, int& gw, int& groups) -> int {
-    const int max_warps = std::min(32, 65536 / std::max(1, regs * 32));
+  auto shape = [&](size_t warp_bytes, int gw_default, int regs, int max_threads, int& gw,
+                   int& groups) -> int {
+    const int max_warps = std::min(max_threads / 32, 65536 / std::max(1, regs * 32));
     gw = o.warps > 0 ? o.warps : gw_default;
     gw = std::min(gw, max_warps);
     for (;;) {
@@ -424,8 +425,12 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       --gw;
     }
   };
-  if ((rc = shape(fw, P->f64 ? 2 : 4, fa_f.numRegs, P->fwd_gw, P->fwd_groups))) return rc;
-  if ((rc = shape(aw, P->f64 ? 2 : 4, fa_a.numRegs, P->adj_gw, P->adj_groups))) return rc;
+  // Defaults measured on the 256-event 128x128x64 workload: the forward
+  // runs two solves of 6 warps per SM (its register cap allows 12 warps), the
+  // adjoint two solves of 4 warps (its tiles allow 9).
+  if ((rc = shape(fw, P->f64 ? 2 : 6, fa_f.numRegs, ADT_FWD_MAXT, P->fwd_gw, P->fwd_groups)))
+    return rc;
+  if ((rc = shape(aw, P->f64 ? 2 : 4, fa_a.numRegs, 1024, P->adj_gw, P->adj_groups))) return rc;
   // verify with the occupancy calculator; shrink until one CTA fits
   auto fits = [&](const void* fn, int gw, int& groups, size_t warp_bytes, size_t& smem) -> int {
     for (;;) {

@@ -16,17 +16,15 @@
 #pragma once
 #include "eik3d_brick.cuh"
 
-// Register budget of the persistent sweep kernels: threads per CTA the
-// compiler must fit (0 = unconstrained).  65536 / ADT_BATCH_MAXT registers
-// per thread.
-#ifndef ADT_BATCH_MAXT
-#define ADT_BATCH_MAXT 0
+// Register budgets of the persistent sweep kernels: threads per CTA the
+// compiler must fit, 65536 / (threads) registers per thread.  The forward
+// tile needs 16 KB of shared memory per warp, so 12 warps (two solves of 6
+// warps) fit an SM when a thread has at most 170 registers; the adjoint
+// tiles (23 KB per warp) hold it to 9 warps, so it is left unconstrained.
+#ifndef ADT_FWD_MAXT
+#define ADT_FWD_MAXT 384
 #endif
-#if ADT_BATCH_MAXT > 0
-#define ADT_BATCH_BOUNDS __launch_bounds__(ADT_BATCH_MAXT, 1)
-#else
-#define ADT_BATCH_BOUNDS
-#endif
+#define ADT_FWD_BOUNDS __launch_bounds__(ADT_FWD_MAXT, 1)
 
 namespace adt {
 
@@ -301,7 +299,7 @@ __device__ __forceinline__ bool dispatch_fwd_f32(float* S, const float* F, const
 }
 
 template <class T, int BK, int MODE>
-__global__ void ADT_BATCH_BOUNDS k_batch_fwd(BatchArgs<T> A) {
+__global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GroupCtx c = group_ctx(A, smem);
   if (c.grp >= c.G) return;
@@ -694,7 +692,7 @@ __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const
 }
 
 template <class T, int BK>
-__global__ void ADT_BATCH_BOUNDS k_batch_adj(BatchArgs<T> A) {
+__global__ void k_batch_adj(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GroupCtx c = group_ctx(A, smem);
   if (c.grp >= c.G) return;

@@ -200,17 +200,16 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
 }
 
 // ---------------------------------------------------------------------------
-// FP32 staging with 16-byte vector loads (grids whose k extent is a multiple
-// of 4, so every brick column segment starts on a 16-byte boundary).  Travel
-// times, adjoint variables and codes are written during the kernel by other
-// warps, so they are read with ordinary (coherent) loads; only the slowness
-// goes through the read-only path.  The 56
-// columns of a halo tile (32 interior, 24 face columns) are split into
-// 4-float chunks; lane t takes chunks t, t+32, ...  Out-of-grid cells of the
-// halo are written as `ghost`: +inf for travel times, so min(neighbour pair)
-// falls back to the single interior neighbour exactly as the reference's edge
-// rule does, and 0 for adjoint variables, whose ghosts are only ever
-// multiplied by a zero weight.
+// FP32 staging for grids whose k extent is a multiple of 4 (every brick
+// column segment starts on a 16-byte boundary).  The 56 columns of a halo
+// tile (32 interior, 24 face columns) are split into 4-float chunks; lane t
+// takes chunks t, t+32, ...  Out-of-grid cells of the halo are written as
+// `ghost`: +inf for travel times, so min(neighbour pair) falls back to the
+// single interior neighbour exactly as the reference's edge rule does, and 0
+// for adjoint variables, whose ghosts are only ever multiplied by a zero
+// weight.  Travel times, adjoint variables and codes are written during the
+// kernel by other warps, so they are read through the coherent path (cp.async
+// and ordinary loads), never the read-only one.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void halo_col(int c, int& ci, int& cj) {
   if (c < BI * BJ) {  // interior
@@ -225,99 +224,6 @@ __device__ __forceinline__ void halo_col(int c, int& ci, int& cj) {
       ci = ((h - 8) & 7) + 1;
       cj = (h < 16) ? 0 : BJ + 1;
     }
-  }
-}
-
-// Global loads of a batch are all issued before any shared store, so a
-// brick pays the memory latency once per batch instead of once per chunk.
-constexpr int LOAD_BATCH = 7;
-
-template <int BK>
-__device__ __forceinline__ void load_tile_f32_vec(float* S, const float* src,
-                                                  const Geom& g, const BrickPos& p, int CS,
-                                                  int lane,
-                                                  float ghost = INFINITY) {
-  constexpr int RS = tile_row_stride(BK);
-  constexpr int CH = BK / 4;
-  constexpr int NCOL = BI * BJ + 2 * BI + 2 * BJ;  // 56
-  constexpr int PER = NCOL * CH / 32;              // chunks per lane (exact)
-  static_assert(NCOL * CH % 32 == 0 && PER % LOAD_BATCH == 0, "tile chunking");
-  const float INF = ghost;
-  // k halo of the interior columns (lane c takes interior column c), issued first
-  const int hci = (lane >> 2) + 1, hcj = (lane & 3) + 1;
-  float hlo = INF, hhi = INF;
-  {
-    const int i = p.i0 + hci - 1, j = p.j0 + hcj - 1;
-    if (i < g.m && j < g.n) {
-      const float* col = src + ((int64_t)i * g.n + j) * g.l + p.k0;
-      if (p.k0 > 0) hlo = col[-1];
-      if (p.k0 + p.nk < g.l) hhi = col[p.nk];
-    }
-  }
-#pragma unroll
-  for (int b0 = 0; b0 < PER; b0 += LOAD_BATCH) {
-    float4 v[LOAD_BATCH];
-    int dst[LOAD_BATCH];
-#pragma unroll
-    for (int t = 0; t < LOAD_BATCH; ++t) {
-      const int e = lane + 32 * (b0 + t);
-      const int c = e / CH, ch = e - (e / CH) * CH;
-      int ci, cj;
-      halo_col(c, ci, cj);
-      const int i = p.i0 + ci - 1, j = p.j0 + cj - 1, k = 4 * ch;
-      v[t] = make_float4(INF, INF, INF, INF);
-      if (i >= 0 && i < g.m && j >= 0 && j < g.n && k < p.nk)
-        v[t] = *reinterpret_cast<const float4*>(src + ((int64_t)i * g.n + j) * g.l + p.k0 + k);
-      dst[t] = ci * RS + cj * CS + 1 + k;
-    }
-#pragma unroll
-    for (int t = 0; t < LOAD_BATCH; ++t) {
-      float* d = S + dst[t];
-      d[0] = v[t].x;
-      d[1] = v[t].y;
-      d[2] = v[t].z;
-      d[3] = v[t].w;
-    }
-  }
-  float* d = S + hci * RS + hcj * CS;
-  d[0] = hlo;
-  d[1 + p.nk] = hhi;
-}
-
-template <int BK>
-__device__ __forceinline__ void load_interior_f32_vec(float* S, const float* __restrict__ src,
-                                                      const Geom& g, const BrickPos& p, int CS,
-                                                      int lane) {
-  constexpr int IRS = itile_row_stride(BK);
-  constexpr int CH = BK / 4;
-  constexpr int PER = BI * BJ * CH / 32;
-  constexpr int NB = PER < 8 ? PER : 8;
-  static_assert(PER % NB == 0, "interior chunking");
-#pragma unroll
-  for (int b0 = 0; b0 < PER; b0 += NB) {
-    float4 v[NB];
-    int dst[NB];
-    bool ok[NB];
-#pragma unroll
-    for (int t = 0; t < NB; ++t) {
-      const int e = lane + 32 * (b0 + t);
-      const int c = e / CH, ch = e - (e / CH) * CH;
-      const int ci = c >> 2, cj = c & 3, k = 4 * ch;
-      ok[t] = ci < p.ni && cj < p.nj && k < p.nk;
-      if (ok[t])
-        v[t] = __ldg(reinterpret_cast<const float4*>(
-            src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k));
-      dst[t] = ci * IRS + cj * CS + k;
-    }
-#pragma unroll
-    for (int t = 0; t < NB; ++t)
-      if (ok[t]) {
-        float* d = S + dst[t];
-        d[0] = v[t].x;
-        d[1] = v[t].y;
-        d[2] = v[t].z;
-        d[3] = v[t].w;
-      }
   }
 }
 
