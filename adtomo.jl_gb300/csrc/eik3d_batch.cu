@@ -646,6 +646,8 @@ int batch_stats(BatchPlan* P, adt_batch_stats* s) {
   s->warps = P->fwd_gw;
   s->groups = P->fwd_groups;
   s->ctas = P->fwd_ctas;
+  s->adj_warps = P->adj_gw;
+  s->adj_groups = P->adj_groups;
   s->fwd_ms = s->adj_ms = s->total_ms = -1.f;
   if (!P->ran) return ADT_OK;
   ADT_CUDA(cudaStreamSynchronize(P->stream));

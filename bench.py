@@ -277,6 +277,7 @@ def run_ours(args, rank, world):
                    "events_per_gpu": N_EVENTS, "grid": [M, N, L], "l2": "inputs larger than L2 "
                    "(1 GB of travel times + 1 GB of adjoint variables per step)",
                    "bk": st.bk, "warps_per_solve": st.warps, "solves_per_cta": st.groups,
+                   "adjoint_warps_per_solve": st.adj_warps, "adjoint_solves_per_cta": st.adj_groups,
                    "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status]))},

@@ -221,6 +221,8 @@ typedef struct adt_batch_stats {
   int32_t warps;  /* warps per solve (group) of the forward kernel */
   int32_t groups; /* solves resident per CTA in the forward kernel */
   int32_t ctas;
+  int32_t adj_warps;  /* the same for the adjoint kernel */
+  int32_t adj_groups;
 } adt_batch_stats;
 int adt_batch_stats_get(adt_batch* b, adt_batch_stats* out);
 
