@@ -87,6 +87,8 @@ SIGNATURES = {
     "adt_batch_stats_get": (C.c_int, [_P, _P]),
     "adt_smooth_l1": (C.c_int, [_P, _I64, _I64, _I64, _I32, _I32, _D, _P, _P]),
     "adt_smooth_l1_device": (C.c_int, [_P, _I64, _I64, _I64, _I32, _I32, _D, _P, _P, _P]),
+    "adt_locate_loss_grad": (C.c_int, [_I32, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _D, _D,
+                                       _D, _P, _D, _P, _P]),
 }
 
 

@@ -18,7 +18,7 @@ CSRC = os.path.join(os.path.dirname(PKG), "csrc")
 BUILD = os.path.join(os.path.dirname(PKG), "_build")
 LIB = os.path.join(PKG, "libadtomo_gpu.so")
 SOURCES = ["capi.cu", "eik2d.cu", "eik3d_single.cu", "eik3d_batch.cu", "eik3d_noalloc.cu",
-           "smooth.cu"]
+           "smooth.cu", "locate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-Xptxas", "-O3"]
 

@@ -241,6 +241,27 @@ int adt_smooth_l1(const double* v, int64_t m, int64_t n, int64_t l, int32_t sh, 
 int adt_smooth_l1_device(const double* v, int64_t m, int64_t n, int64_t l, int32_t sh,
                          int32_t sv, double lambda, double* penalty, double* grad, void* stream);
 
+/* ------------------------------------------------------------------------
+ * 2D-table event location (replaces the torch closure of
+ * tests/Eikonal/eikoloc.py:157-206): for every event e, at params[4e..4e+3]
+ * = (t0, x, y, z), the loss
+ *   mean over its P picks of w huber(t - (t0 + T_P(r, |z| - z_sta)))
+ *   + the same over its S picks
+ *   + gamma * mean over pick pairs of one phase of w_i w_j huber(dT_ij - dt_ij)
+ * and its gradient with respect to (t0, x, y, z).  Picks of event e are
+ * [offs[e], offs[e+1]) of sta_xyz (3 per pick), t_obs, phase (0 = P,
+ * 1 = S) and weight.  table_p/table_s: m x n travel times on the grid
+ * r = r0 + i h, z = z0 + j h, read bilinearly with the cell clamped to the
+ * table (eikoloc.py:119-145).  bounds: (xmin, xmax, ymin, ymax, zmin, zmax);
+ * the position is clamped to them (a clamped coordinate has no gradient).
+ * huber: delta 1 (torch's default).  With gamma != 0 an event may have at most
+ * 256 picks.  FP64; host pointers; loss (n_events), grad (4 n_events) out. */
+int adt_locate_loss_grad(int32_t n_events, const double* params, const int64_t* offs,
+                         const double* sta_xyz, const double* t_obs, const int32_t* phase,
+                         const double* weight, const double* table_p, const double* table_s,
+                         int32_t m, int32_t n, double r0, double z0, double h,
+                         const double* bounds, double gamma, double* loss, double* grad);
+
 #ifdef __cplusplus
 }
 #endif
