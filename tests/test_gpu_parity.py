@@ -334,3 +334,27 @@ def test_batch_fp32_mixed_fields_alignment():
         assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
     assert all(s.converged and s.adj_converged for s in st)
     B.close()
+
+
+def test_batch_many_bricks_global_meta():
+    """A grid with more bricks (33 x 65 x 1 = 2145) than the per-group
+    shared-memory metadata holds, so brick timestamps live in global memory,
+    as on the 256x256x128 grids of the largest configuration: FP64 with the
+    reference stopping rule bit-exact, FP32 within tolerance."""
+    rng = np.random.default_rng(13)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(264, 260, 8, 0.5)], 2, 10)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, ito = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-6, 20)
+    assert np.array_equal(tp, tpo) and mis == mo
+    assert np.array_equal(grads[0], go[0])
+    assert [s.iters for s in st] == list(ito)
+    B.close()
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4
+    assert np.linalg.norm(grads[0] - go[0]) <= 1e-3 * np.linalg.norm(go[0])
+    assert all(s.converged and s.adj_converged for s in st)
+    B.close()
