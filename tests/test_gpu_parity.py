@@ -253,6 +253,7 @@ def test_batch_chunking_and_graph_do_not_change_results():
         assert out[0] == r[0], kw
         assert np.array_equal(out[1], r[1]), kw
         assert np.array_equal(out[2][0], r[2][0]), kw
+        assert [(x.iters, x.adj_iters) for x in out[3]] == [(x.iters, x.adj_iters) for x in r[3]], kw
         # a second evaluation of the same plan reproduces the first
         out2 = B.run(slow, t_obs, w)
         assert np.array_equal(out2[2][0], out[2][0]), kw
