@@ -211,6 +211,13 @@ class Batch3D:
     def stream(self) -> int:
         return self._L.adt_batch_stream(self._h) or 0
 
+    def autotune(self, reps: int = 2) -> BatchStats:
+        """Time the sweep kernels over candidate launch shapes on the uploaded
+        inputs and keep the fastest (adt_batch_autotune); returns the stats
+        of the chosen shape."""
+        check(self._L.adt_batch_autotune(self._h, int(reps)))
+        return self.stats()
+
     def stats(self) -> BatchStats:
         s = BatchStats()
         check(self._L.adt_batch_stats_get(self._h, C.byref(s)))

@@ -306,6 +306,11 @@ int adt_batch_set_source_slowness(adt_batch* b, const double* slowness0) {
   return batch_set_source_slowness(b->plan, slowness0);
 }
 
+int adt_batch_autotune(adt_batch* b, int32_t reps) {
+  if (!b) return set_error(ADT_EINVAL, "batch: null handle");
+  return batch_autotune(b->plan, reps);
+}
+
 int adt_batch_run_resident(adt_batch* b) {
   if (!b) return set_error(ADT_EINVAL, "batch: null handle");
   return batch_run_resident(b->plan);

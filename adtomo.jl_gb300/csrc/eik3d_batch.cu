@@ -139,12 +139,15 @@ struct BatchPlan {
   DevBuf d_gdense;  // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
   int64_t snap_stride = 0;
   std::vector<adt_solve_status> h_status;
+  int uploaded = 0;  // bits: 1 slowness, 2 t_obs, 4 weight
   bool src_fixed = false;  // near-source values from d_slow0 (batch_set_source_slowness)
   // launch shapes
   KernelSet ks;
   int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
   int fwd_gw = 4, fwd_groups = 2, adj_gw = 2, adj_groups = 4;
   int max_nb = 0, meta_smem = 0;
+  int sm_count = 0, fwd_regs = 0, adj_regs = 0;
+  size_t smem_budget = 0, fwd_wbytes = 0, adj_wbytes = 0;
   size_t fwd_smem = 0, adj_smem = 0, mis_smem = 0;
   // graph and timing
   cudaGraphExec_t graph = nullptr;
@@ -173,6 +176,70 @@ void batch_opts_default(adt_batch_opts* o) {
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
+
+// Launch shape of one sweep kernel: `gw` warps per solve (warp group) and as
+// many groups per CTA as shared memory, registers and `max_threads` allow
+// (at most `groups_req` when > 0); confirmed with the occupancy calculator.
+static int fit_shape(const void* fn, size_t warp_bytes, int regs, int max_threads, int meta_smem,
+                     int max_nb, size_t budget, int gw_req, int groups_req, int& gw, int& groups,
+                     size_t& smem) {
+  const int max_warps = std::min(max_threads / 32, 65536 / std::max(1, regs * 32));
+  gw = std::max(1, std::min(gw_req, max_warps));
+  for (;;) {
+    int G = 1;
+    while (G < 15 &&
+           group_hdr_bytes(G + 1, meta_smem, max_nb) + (size_t)(G + 1) * gw * warp_bytes <= budget &&
+           (G + 1) * gw <= max_warps)
+      ++G;
+    if (group_hdr_bytes(G, meta_smem, max_nb) + (size_t)G * gw * warp_bytes <= budget) {
+      if (groups_req > 0) G = std::min(G, groups_req);
+      for (;;) {  // shrink until one CTA fits
+        smem = group_hdr_bytes(G, meta_smem, max_nb) + (size_t)G * gw * warp_bytes;
+        ADT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int occ = 0;
+        ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, G * gw * 32, smem));
+        if (occ >= 1) break;
+        if (G == 1) return set_error(ADT_EINVAL, "batch: no launch shape fits on this device");
+        --G;
+      }
+      groups = G;
+      return ADT_OK;
+    }
+    if (gw == 1) return set_error(ADT_EINVAL, "batch: brick tile does not fit in shared memory");
+    --gw;
+  }
+}
+
+// Set both sweep kernels' launch shapes (0 = default width / as many groups
+// as fit) and drop a captured graph that used the old ones.  Defaults,
+// measured on the 256-event 128x128x64 workload: the forward runs two solves
+// of 6 warps per SM (its register cap allows 12 warps), the adjoint two
+// solves of 4 warps (its tiles allow 9).
+static int apply_shapes(BatchPlan* P, int fwd_gw, int fwd_groups, int adj_gw, int adj_groups) {
+  int rc;
+  if ((rc = fit_shape(P->ks.fwd, P->fwd_wbytes, P->fwd_regs, ADT_FWD_MAXT, P->meta_smem, P->max_nb,
+                      P->smem_budget, fwd_gw > 0 ? fwd_gw : (P->f64 ? 2 : 6), fwd_groups,
+                      P->fwd_gw, P->fwd_groups, P->fwd_smem)))
+    return rc;
+  if ((rc = fit_shape(P->ks.adj, P->adj_wbytes, P->adj_regs, 1024, P->meta_smem, P->max_nb,
+                      P->smem_budget, adj_gw > 0 ? adj_gw : (P->f64 ? 2 : 4), adj_groups,
+                      P->adj_gw, P->adj_groups, P->adj_smem)))
+    return rc;
+  P->fwd_warps = P->fwd_gw * P->fwd_groups;
+  P->adj_warps = P->adj_gw * P->adj_groups;
+  int occ_f = 0, occ_a = 0;
+  ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, P->ks.fwd, P->fwd_warps * 32,
+                                                         P->fwd_smem));
+  ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, P->ks.adj, P->adj_warps * 32,
+                                                         P->adj_smem));
+  P->fwd_ctas = std::max(1, occ_f) * P->sm_count;
+  P->adj_ctas = std::max(1, occ_a) * P->sm_count;
+  if (P->graph) {
+    cudaGraphExecDestroy(P->graph);
+    P->graph = nullptr;
+  }
+  return ADT_OK;
+}
 
 int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* hh,
                  const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
@@ -395,69 +462,28 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     if (!uo.empty()) ADT_CUDA(cudaMemcpy(P->d_uoff.p, uo.data(), uo.size() * 8, cudaMemcpyHostToDevice));
   }
   // launch shapes: warp groups (one solve each) per CTA, as many as fit
-  int sm_count = 0, smem_optin = 0;
-  ADT_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, P->dev));
+  ADT_CUDA(cudaDeviceGetAttribute(&P->sm_count, cudaDevAttrMultiProcessorCount, P->dev));
+  int smem_optin = 0;
   ADT_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->dev));
-  const size_t budget = (size_t)smem_optin - 1024;
-  const size_t fw = P->f64 ? fwd_warp_smem<double>(P->bk) : fwd_warp_smem<float>(P->bk);
-  const size_t aw = P->f64 ? adj_warp_smem<double>(P->bk) : adj_warp_smem<float>(P->bk);
+  P->smem_budget = (size_t)smem_optin - 1024;
+  P->fwd_wbytes = P->f64 ? fwd_warp_smem<double>(P->bk) : fwd_warp_smem<float>(P->bk);
+  P->adj_wbytes = P->f64 ? adj_warp_smem<double>(P->bk) : adj_warp_smem<float>(P->bk);
   for (auto& g : P->geoms) P->max_nb = std::max(P->max_nb, g.nbx * g.nby * g.nbz);
   P->meta_smem = ((size_t)META_ARRAYS * P->max_nb * sizeof(int) <= 16384) ? 1 : 0;
-  cudaFuncAttributes fa_f, fa_a;
-  ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
-  ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
-  auto shape = [&](size_t warp_bytes, int gw_default, int regs, int max_threads, int& gw,
-                   int& groups) -> int {
-    const int max_warps = std::min(max_threads / 32, 65536 / std::max(1, regs * 32));
-    gw = o.warps > 0 ? o.warps : gw_default;
-    gw = std::min(gw, max_warps);
-    for (;;) {
-      int G = 1;
-      while (G < 15 && group_hdr_bytes(G + 1, P->meta_smem, P->max_nb) + (size_t)(G + 1) * gw * warp_bytes <= budget &&
-             (G + 1) * gw <= max_warps)
-        ++G;
-      if (group_hdr_bytes(G, P->meta_smem, P->max_nb) + (size_t)G * gw * warp_bytes <= budget) {
-        if (o.groups > 0) G = std::min(G, (int)o.groups);
-        groups = G;
-        return ADT_OK;
-      }
-      if (gw == 1) return set_error(ADT_EINVAL, "batch: brick tile does not fit in shared memory");
-      --gw;
-    }
-  };
-  // Defaults measured on the 256-event 128x128x64 workload: the forward
-  // runs two solves of 6 warps per SM (its register cap allows 12 warps), the
-  // adjoint two solves of 4 warps (its tiles allow 9).
-  if ((rc = shape(fw, P->f64 ? 2 : 6, fa_f.numRegs, ADT_FWD_MAXT, P->fwd_gw, P->fwd_groups)))
-    return rc;
-  if ((rc = shape(aw, P->f64 ? 2 : 4, fa_a.numRegs, 1024, P->adj_gw, P->adj_groups))) return rc;
-  // verify with the occupancy calculator; shrink until one CTA fits
-  auto fits = [&](const void* fn, int gw, int& groups, size_t warp_bytes, size_t& smem) -> int {
-    for (;;) {
-      smem = group_hdr_bytes(groups, P->meta_smem, P->max_nb) + (size_t)groups * gw * warp_bytes;
-      ADT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      int occ = 0;
-      ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, groups * gw * 32, smem));
-      if (occ >= 1) return ADT_OK;
-      if (groups == 1) return set_error(ADT_EINVAL, "batch: no launch shape fits on this device");
-      --groups;
-    }
-  };
-  if ((rc = fits(P->ks.fwd, P->fwd_gw, P->fwd_groups, fw, P->fwd_smem))) return rc;
-  if ((rc = fits(P->ks.adj, P->adj_gw, P->adj_groups, aw, P->adj_smem))) return rc;
-  P->fwd_warps = P->fwd_gw * P->fwd_groups;
-  P->adj_warps = P->adj_gw * P->adj_groups;
+  {
+    cudaFuncAttributes fa_f, fa_a;
+    ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
+    ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
+    P->fwd_regs = fa_f.numRegs;
+    P->adj_regs = fa_a.numRegs;
+  }
+  if ((rc = apply_shapes(P.get(), o.warps, o.groups, o.warps, o.groups))) return rc;
   int maxsta = 0;
   for (int f = 0; f < n_fields; ++f) maxsta = std::max(maxsta, P->nsta[f]);
   int pw = 1;
   while (pw < 8 * maxsta) pw <<= 1;
   P->mis_smem = (size_t)pw * 16 + (size_t)maxsta * 8 + 16;
   ADT_CUDA(cudaFuncSetAttribute(P->ks.misfit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->mis_smem));
-  int occ_f = 0, occ_a = 0;
-  ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, P->ks.fwd, P->fwd_warps * 32, P->fwd_smem));
-  ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, P->ks.adj, P->adj_warps * 32, P->adj_smem));
-  P->fwd_ctas = std::max(1, occ_f) * sm_count;
-  P->adj_ctas = std::max(1, occ_a) * sm_count;
   if (P->opts.ref_compat) {
     int64_t maxc = 0;
     for (auto& g : P->geoms) maxc = std::max(maxc, g.ncell);
@@ -577,10 +603,66 @@ int batch_upload(BatchPlan* P, const double* slowness, const double* t_obs, cons
       if (!(slowness[i] > 0.0) || !std::isfinite(slowness[i]))
         return set_error(ADT_EINVAL, "batch: slowness must be finite and > 0 (cell %lld)", (long long)i);
     ADT_CUDA(cudaMemcpyAsync(P->d_slow64.p, slowness, P->ncell_total * 8, cudaMemcpyHostToDevice, P->stream));
+    P->uploaded |= 1;
   }
-  if (t_obs) ADT_CUDA(cudaMemcpyAsync(P->d_tobs.p, t_obs, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
-  if (weight) ADT_CUDA(cudaMemcpyAsync(P->d_w.p, weight, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
+  if (t_obs) {
+    ADT_CUDA(cudaMemcpyAsync(P->d_tobs.p, t_obs, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
+    P->uploaded |= 2;
+  }
+  if (weight) {
+    ADT_CUDA(cudaMemcpyAsync(P->d_w.p, weight, P->nobs * 8, cudaMemcpyHostToDevice, P->stream));
+    P->uploaded |= 4;
+  }
   return ADT_OK;
+}
+
+// Pick the sweep kernels' group widths by timing them on the uploaded
+// inputs: every candidate width runs `reps` evaluations and the fastest
+// forward and adjoint kernel times (CUDA events around each kernel) win; the
+// two kernels are tuned one after the other.  Results do not depend on the
+// shape (the bricks of a level are independent), only the time does.
+int batch_autotune(BatchPlan* P, int reps) {
+  if (P->opts.ref_compat)
+    return set_error(ADT_EINVAL, "batch: autotune is not available with ref_compat");
+  if ((P->uploaded & 7) != 7)
+    return set_error(ADT_EINVAL, "batch: upload slowness, t_obs and weight before autotune");
+  reps = std::max(1, std::min(reps, 16));
+  const int fwd_c[] = {3, 4, 5, 6, 8, 12};
+  const int adj_c[] = {2, 3, 4, 6, 8};
+  auto measure = [&](float& fwd_ms, float& adj_ms) -> int {
+    fwd_ms = adj_ms = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+      int rc = batch_run_resident(P);
+      if (rc) return rc;
+      ADT_CUDA(cudaStreamSynchronize(P->stream));
+      adt_batch_stats st;
+      if ((rc = batch_stats(P, &st))) return rc;
+      fwd_ms = std::min(fwd_ms, st.fwd_ms);
+      adj_ms = std::min(adj_ms, st.adj_ms);
+    }
+    return ADT_OK;
+  };
+  int rc, best_f = P->fwd_gw, best_a = P->adj_gw;
+  float best_ft = 1e30f, best_at = 1e30f, ft, at;
+  for (int gw : fwd_c) {
+    if ((rc = apply_shapes(P, gw, 0, best_a, 0))) return rc;
+    if (P->fwd_gw != gw) continue;  // did not fit
+    if ((rc = measure(ft, at))) return rc;
+    if (ft < best_ft) {
+      best_ft = ft;
+      best_f = gw;
+    }
+  }
+  for (int gw : adj_c) {
+    if ((rc = apply_shapes(P, best_f, 0, gw, 0))) return rc;
+    if (P->adj_gw != gw) continue;
+    if ((rc = measure(ft, at))) return rc;
+    if (at < best_at) {
+      best_at = at;
+      best_a = gw;
+    }
+  }
+  return apply_shapes(P, best_f, 0, best_a, 0);
 }
 
 int batch_set_source_slowness(BatchPlan* P, const double* slowness0) {

@@ -14,6 +14,7 @@ void batch_destroy(BatchPlan* p);
 int batch_upload(BatchPlan* p, const double* slowness, const double* t_obs, const double* weight);
 int batch_run_resident(BatchPlan* p);
 int batch_set_source_slowness(BatchPlan* p, const double* slowness0);
+int batch_autotune(BatchPlan* p, int reps);
 int batch_download(BatchPlan* p, double* misfit, double* t_pred, double* grad,
                    adt_solve_status* status);
 int batch_stats(BatchPlan* p, adt_batch_stats* s);

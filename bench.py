@@ -194,6 +194,8 @@ def run_ours(args, rank, world):
     B.run_resident()
     _, t_obs, _, _ = B.download()
     B.upload([f], t_obs, w)
+    if args.autotune and not (args.warps or args.groups):
+        B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
     stream = torch.cuda.ExternalStream(B.stream())
     for _ in range(args.warmup):
         B.run_resident()
@@ -278,6 +280,8 @@ def run_ours(args, rank, world):
                    "(1 GB of travel times + 1 GB of adjoint variables per step)",
                    "bk": st.bk, "warps_per_solve": st.warps, "solves_per_cta": st.groups,
                    "adjoint_warps_per_solve": st.adj_warps, "adjoint_solves_per_cta": st.adj_groups,
+                   "shapes": "autotuned" if args.autotune and not (args.warps or args.groups)
+                   else "fixed",
                    "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status]))},
@@ -305,6 +309,79 @@ def run_ours(args, rank, world):
     B.close()
 
 
+def large_workload(name, rng):
+    """The uneven P/S batch (C4) and the inversion-scale grid (C5)."""
+    from adtomo_gb300 import synth
+    if name == "c4":
+        fields, stations, slow, sf, src = [], [], [], [], []
+        for gi, (m, n, l) in enumerate([(64, 64, 32), (96, 96, 48), (128, 128, 64), (160, 160, 80)]):
+            vp = synth.layered_smooth(m, n, l, rng)
+            sta = synth.surface_stations(m, n, 150, rng)
+            for v in (vp, vp / 1.73):
+                fields.append((m, n, l, 0.5))
+                slow.append(1.0 / v)
+                stations.append(sta)
+            for e in synth.volume_sources(m, n, l, 128, rng):
+                for ph in range(2):
+                    sf.append(2 * gi + ph)
+                    src.append(e)
+        desc = ("C4: 512 events on grids 64x64x32, 96x96x48, 128x128x64, 160x160x80 (h=0.5 km), "
+                "P and S fields each (Vp layered 4-8 km/s x (1+-5%) smooth, Vs = Vp/1.73), "
+                "1024 solves, 150 surface stations per grid, gradients wrt all 8 slownesses")
+        return fields, stations, slow, np.array(sf, np.int32), np.array(src), 0, desc
+    m, n, l = 256, 256, 128
+    f = synth.layered_checkerboard(m, n, l, block=8)
+    sta = synth.surface_stations(m, n, 300, rng)
+    src = synth.volume_sources(m, n, l, 2000, rng)
+    desc = ("C5: 2000 events on 256x256x128, h=0.25 km, layered+checkerboard, 300 surface "
+            "stations, forward fields recomputed per 128-event chunk")
+    return [(m, n, l, 0.25)], [sta], [f], np.zeros(2000, np.int32), src, 128, desc
+
+
+def run_large(args):
+    """Secondary lines for the larger configurations (not the headline)."""
+    import torch
+    import adtomo_gb300 as A
+    rng = np.random.default_rng(SEED)
+    fields, stations, slow, sf, src, chunk, desc = large_workload(args.workload, rng)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, chunk=chunk)
+    n_obs = sum(len(stations[f]) for f in sf)
+    B.upload(slow, np.full(n_obs, 1.0), np.ones(n_obs))
+    B.run_resident()
+    _, tp, _, _ = B.download()  # picks from the model itself, then a 2% slower model
+    B.upload([s * 1.02 for s in slow], tp, np.ones(n_obs))
+    if args.autotune:
+        B.autotune(reps=1)
+    for _ in range(args.warmup):
+        B.run_resident()
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(B.stream())
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(args.steps):
+            B.run_resident()
+        end.record(stream)
+    torch.cuda.synchronize()
+    ms_step = start.elapsed_time(end) / args.steps
+    mis, tp, grads, status = B.download()
+    st = B.stats()
+    line = {
+        "metric": METRIC, "value": len(sf) / (ms_step / 1000.0), "unit": "solves/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "solves": int(len(sf)), "chunk": chunk,
+                   "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
+                   "cell_updates_per_s": (st.fwd_cell_updates + st.adj_cell_updates) /
+                   (ms_step / 1000.0),
+                   "fwd_iters_mean": float(np.mean([x.iters for x in status])),
+                   "adj_iters_mean": float(np.mean([x.adj_iters for x in status])),
+                   "all_converged": bool(all(x.converged and x.adj_converged for x in status))},
+    }
+    print(json.dumps(line), flush=True)
+    B.close()
+
+
 def main():
     global N_EVENTS
     ap = argparse.ArgumentParser()
@@ -317,6 +394,11 @@ def main():
     ap.add_argument("--bk", type=int, default=0, help="brick depth (0 = library default)")
     ap.add_argument("--warps", type=int, default=0, help="warps per solve (0 = default)")
     ap.add_argument("--groups", type=int, default=0, help="solves per CTA (0 = as many as fit)")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: time candidate launch shapes on the workload first (untimed setup)")
+    ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5"],
+                    help="c3 (default): the headline; c4, c5: secondary lines for the larger "
+                         "configurations")
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,
@@ -327,6 +409,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "c3":
+        if rank == 0:
+            run_large(args)
         return
     if world > 1:
         import torch.distributed as dist

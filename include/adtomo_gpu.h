@@ -191,6 +191,13 @@ int adt_batch_run(adt_batch* b, const double* slowness, const double* t_obs, con
  * evaluation either way: the gradient does not flow through them. */
 int adt_batch_set_source_slowness(adt_batch* b, const double* slowness0);
 
+/* Autotuner of the launch shapes: after adt_batch_upload of all three
+ * inputs, times the forward and the adjoint sweep kernels over candidate
+ * warp-group widths (reps evaluations each, 1-16) on those inputs and keeps
+ * the fastest of each (visible in adt_batch_stats_get).  Results do not
+ * depend on the shape.  Not available with ref_compat. */
+int adt_batch_autotune(adt_batch* b, int32_t reps);
+
 /* Device-resident use: upload inputs once, run, read outputs later.  upload
  * takes host pointers (NULL leaves that input unchanged); run_resident enqueues
  * one evaluation on the plan's stream without synchronising; download copies

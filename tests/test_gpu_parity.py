@@ -359,3 +359,25 @@ def test_batch_many_bricks_global_meta():
     assert np.linalg.norm(grads[0] - go[0]) <= 1e-3 * np.linalg.norm(go[0])
     assert all(s.converged and s.adj_converged for s in st)
     B.close()
+
+
+def test_batch_autotune_keeps_results():
+    rng = np.random.default_rng(14)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(32, 24, 16, 0.5)], 6, 8)
+    ref = A.Batch3D(fields, stations, sf, src)
+    r = ref.run(slow, t_obs, w)
+    B = A.Batch3D(fields, stations, sf, src)
+    with pytest.raises(A.AdtError):
+        B.autotune()  # inputs not uploaded yet
+    B.upload(slow, t_obs, w)
+    st = B.autotune(reps=1)
+    assert st.warps >= 1 and st.groups >= 1 and st.adj_warps >= 1 and st.adj_groups >= 1
+    out = B.run(slow, t_obs, w)
+    assert out[0] == r[0] and np.array_equal(out[1], r[1]) and np.array_equal(out[2][0], r[2][0])
+    B.close()
+    ref.close()
+    P = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, ref_compat=True)
+    P.upload(slow, t_obs, w)
+    with pytest.raises(A.AdtError):
+        P.autotune()
+    P.close()
