@@ -137,6 +137,8 @@ struct BatchPlan {
   DevBuf d_levels, d_lstart, d_fields, d_solves, d_order, d_uoff;
   DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
   DevBuf d_gdense;  // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
+  DevBuf d_mis_scratch;  // seed merge arrays when they exceed shared memory
+  int64_t mis_stride = 0;
   int64_t snap_stride = 0;
   std::vector<adt_solve_status> h_status;
   int uploaded = 0;  // bits: 1 slowness, 2 t_obs, 4 weight
@@ -270,8 +272,9 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       return set_error(ADT_EINVAL, "batch: field %d has bad dimensions %d x %d x %d", f, m, n, l);
     if (!(hh[f] > 0.0) || !std::isfinite(hh[f]))
       return set_error(ADT_EINVAL, "batch: field %d has bad spacing", f);
-    if (nsta[f] < 0 || nsta[f] > 1024)
-      return set_error(ADT_EINVAL, "batch: field %d has %d receivers (0..1024 supported)", f, nsta[f]);
+    if (nsta[f] < 0 || nsta[f] > ADT_BATCH_MAX_RECEIVERS)
+      return set_error(ADT_EINVAL, "batch: field %d has %d receivers (0..%d supported)", f,
+                       nsta[f], ADT_BATCH_MAX_RECEIVERS);
     minl = std::min(minl, l);
   }
   (void)minl;
@@ -483,6 +486,13 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   int pw = 1;
   while (pw < 8 * maxsta) pw <<= 1;
   P->mis_smem = (size_t)pw * 16 + (size_t)maxsta * 8 + 16;
+  if (P->mis_smem > 160 * 1024) {  // merge arrays in global scratch, one slice per chunk solve
+    P->mis_stride = (int64_t)((P->mis_smem + 255) / 256 * 256);
+    int cmax = 0;
+    for (auto& ch : P->chunks) cmax = std::max(cmax, ch.count);
+    R_(P->d_mis_scratch, (size_t)P->mis_stride * cmax);
+    P->mis_smem = 0;
+  }
   ADT_CUDA(cudaFuncSetAttribute(P->ks.misfit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->mis_smem));
   if (P->opts.ref_compat) {
     int64_t maxc = 0;
@@ -564,7 +574,9 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
       const double* w = P.d_w.as<double>();
       double* tp = P.d_tpred.as<double>();
       double* sm = P.d_smis.as<double>();
-      void* args[] = {&Af, &tobs, &w, &tp, &sm};
+      unsigned char* scr = P.mis_stride ? P.d_mis_scratch.as<unsigned char>() : nullptr;
+      int64_t stride = P.mis_stride;
+      void* args[] = {&Af, &tobs, &w, &tp, &sm, &scr, &stride};
       ADT_CUDA(cudaLaunchKernel(P.ks.misfit, dim3(ch.count), dim3(256), args, P.mis_smem, st));
     }
     ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 2], st, evf));

@@ -436,11 +436,19 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
 // (missing picks t_obs == -1 skipped, :81) and the sensitivities dL/du at
 // the (up to 8) nodes of each receiver; equal nodes are merged in
 // (receiver, node) order so the seed values are independent of scheduling.
+//
+// The merge arrays live in shared memory, or, for receiver counts too large
+// for it (scratch != null), in a per-CTA slice of global scratch of
+// `scratch_stride` bytes; the bitonic sort is the same either way.
+static_assert(8LL * ADT_BATCH_MAX_RECEIVERS <= (1LL << 20), "merge key entry field");
+
 template <class T>
 __global__ void k_batch_misfit(BatchArgs<T> A, const double* __restrict__ t_obs,
                                const double* __restrict__ weight, double* __restrict__ t_pred,
-                               double* __restrict__ solve_misfit) {
-  extern __shared__ __align__(16) unsigned char smem[];
+                               double* __restrict__ solve_misfit, unsigned char* scratch,
+                               int64_t scratch_stride) {
+  extern __shared__ __align__(16) unsigned char smem_dyn[];
+  unsigned char* smem = scratch ? scratch + (int64_t)blockIdx.x * scratch_stride : smem_dyn;
   const int gs = A.order[blockIdx.x];
   const SolveDev sd = A.solves[gs];
   const FieldDev<T> fd = A.fields[sd.field];
@@ -510,7 +518,8 @@ __global__ void k_batch_misfit(BatchArgs<T> A, const double* __restrict__ t_obs,
           const double v = __dmul_rn(dt, wt);
           const long long cell = ((long long)xi[a] * g.n + yi[b]) * g.l + zi[c];
           // zero contributions leave the accumulated value unchanged: drop them
-          key[e] = (v == 0.0) ? LLONG_MAX : (cell << 16) | e;
+          // (cell, entry) in one key: entry < 8 * ADT_BATCH_MAX_RECEIVERS = 2^19
+          key[e] = (v == 0.0) ? LLONG_MAX : (cell << 20) | e;
           val[e] = v;
         }
   }
@@ -547,7 +556,7 @@ __global__ void k_batch_misfit(BatchArgs<T> A, const double* __restrict__ t_obs,
     for (int e = 0; e < P; ++e) {
       const long long kk = key[e];
       if (kk == LLONG_MAX) break;
-      const long long cell = kk >> 16;
+      const long long cell = kk >> 20;
       if (cell != cur) {
         if (cur >= 0) {
           sidx[ns] = cur;

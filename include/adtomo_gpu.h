@@ -149,6 +149,9 @@ int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double
  * --------------------------------------------------------------------- */
 #define ADT_F32 0
 #define ADT_F64 1
+/* Receivers per field.  Up to 1024 the seed merge runs in shared memory;
+ * above, in device scratch of about 128 bytes per receiver per resident solve. */
+#define ADT_BATCH_MAX_RECEIVERS 65536
 
 typedef struct adt_batch_opts {
   int32_t precision;    /* ADT_F32 (default) or ADT_F64 */

@@ -381,3 +381,32 @@ def test_batch_autotune_keeps_results():
     with pytest.raises(A.AdtError):
         P.autotune()
     P.close()
+
+
+def test_batch_many_receivers_global_merge():
+    """More receivers per field (1500) than the shared-memory seed merge takes,
+    as when events are the receivers (scripts/inversion.jl uses stations as
+    sources): FP64 bit-exact, FP32 within tolerance."""
+    rng = np.random.default_rng(15)
+    m, n, l, h = 40, 36, 16, 0.5
+    slow = [synth.layered_checkerboard(m, n, l, block=4)]
+    rec = np.c_[rng.uniform(0, m - 1, 1500), rng.uniform(0, n - 1, 1500), rng.uniform(0, l - 1, 1500)]
+    rec[:40] = np.round(rec[:40])  # integer positions share nodes with neighbours
+    src = synth.surface_stations(m, n, 3, rng)
+    sf = np.zeros(3, np.int32)
+    t_obs = rng.uniform(0.5, 3.0, 4500)
+    t_obs[rng.random(4500) < 0.1] = -1.0
+    w = rng.uniform(0.5, 1.0, 4500)
+    fields = [(m, n, l, h)]
+    B = A.Batch3D(fields, [rec], sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, _ = oracle_batch(fields, [rec], slow, sf, src, t_obs, w, 1e-6, 20)
+    assert np.array_equal(tp, tpo) and mis == mo and np.array_equal(grads[0], go[0])
+    B.close()
+    B = A.Batch3D(fields, [rec], sf, src, precision=A.ADT_F32, tol=1e-7)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, _ = oracle_batch(fields, [rec], slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4
+    assert np.linalg.norm(grads[0] - go[0]) <= 1e-3 * np.linalg.norm(go[0])
+    B.close()
