@@ -382,6 +382,59 @@ def run_large(args):
     B.close()
 
 
+def run_inversion(args):
+    """10 L-BFGS iterations of the inversion driver in FP32 and in FP64 on the
+    C3 grid, stations as sources (scripts/inversion.jl): time per iteration
+    and the FP32 model's distance from the FP64 one (secondary line)."""
+    import torch  # noqa: F401  (CUDA context through the library)
+    import adtomo_gb300 as A
+    from adtomo_gb300 import synth
+    from adtomo_gb300.inversion import TravelTimeInversion
+    rng = np.random.default_rng(SEED)
+    f_true = synth.layered_checkerboard(M, N, L, block=8)
+    v_true = 1.0 / f_true
+    vel0 = np.broadcast_to(v_true.mean(axis=(0, 1), keepdims=True), v_true.shape).copy()
+    sta = synth.surface_stations(M, N, N_STA, rng)
+    eve = synth.volume_sources(M, N, L, N_EVENTS, rng)
+    P = A.Batch3D([(M, N, L, H)], [eve], np.zeros(N_STA, np.int32), sta, precision=A.ADT_F64,
+                  tol=1e-9, max_iter=200)
+    _, tp, _, _ = P.run([f_true], np.full(N_STA * N_EVENTS, 1.0), np.ones(N_STA * N_EVENTS))
+    P.close()
+    uobs = tp.reshape(N_STA, N_EVENTS)
+    qua = np.ones_like(uobs)
+    out = {}
+    for name, prec in (("f32", A.ADT_F32), ("f64", A.ADT_F64)):
+        inv = TravelTimeInversion((M, N, L, H), vel0, sta, eve, uobs, qua, lambda_p=0.0,
+                                  tol=1e-6, max_iter=200, precision=prec)
+        t0 = time.perf_counter()
+        x, loss, hist = inv.optimize(iterations=args.steps)
+        dt = time.perf_counter() - t0
+        out[name] = {"x": x, "loss": loss, "hist": hist, "s_per_iter": dt / max(len(hist), 1),
+                     "evaluations": inv.evaluations, "v": inv.velocity(x)}
+        inv.close()
+    dv64 = np.linalg.norm(out["f64"]["v"] - vel0)
+    line = {
+        "metric": "L-BFGS time per iteration (s) and FP32-vs-FP64 model difference",
+        "value": out["f32"]["s_per_iter"], "unit": "s/iteration", "n_gpus": 1,
+        "steps": args.steps, "higher_is_better": False, "dtype": "f32",
+        "data": "synthetic (seeded): true layered+checkerboard, start = its depth average",
+        "config": {"workload": f"inversion: 128x128x64, h=0.5 km, {N_STA} stations as sources, "
+                               f"{N_EVENTS} events as receivers, {args.steps} L-BFGS iterations",
+                   "f32_s_per_iteration": out["f32"]["s_per_iter"],
+                   "f64_s_per_iteration": out["f64"]["s_per_iter"],
+                   "f32_evaluations": out["f32"]["evaluations"],
+                   "f64_evaluations": out["f64"]["evaluations"],
+                   "f32_loss": out["f32"]["hist"], "f64_loss": out["f64"]["hist"],
+                   "model_update_rel_diff": float(np.linalg.norm(out["f32"]["v"] - out["f64"]["v"])
+                                                  / max(dv64, 1e-300)),
+                   "model_error_f32": float(np.linalg.norm(out["f32"]["v"] - v_true) /
+                                            np.linalg.norm(vel0 - v_true)),
+                   "model_error_f64": float(np.linalg.norm(out["f64"]["v"] - v_true) /
+                                            np.linalg.norm(vel0 - v_true))},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global N_EVENTS
     ap = argparse.ArgumentParser()
@@ -396,7 +449,7 @@ def main():
     ap.add_argument("--groups", type=int, default=0, help="solves per CTA (0 = as many as fit)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: time candidate launch shapes on the workload first (untimed setup)")
-    ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5", "inversion"],
                     help="c3 (default): the headline; c4, c5: secondary lines for the larger "
                          "configurations")
     ap.add_argument("--plain-sample", type=int, default=4,
@@ -409,6 +462,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "inversion":
+        if rank == 0:
+            run_inversion(args)
         return
     if args.workload != "c3":
         if rank == 0:
