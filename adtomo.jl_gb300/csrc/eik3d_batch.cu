@@ -29,9 +29,11 @@ __global__ void k_to_t_f32(const double* __restrict__ a, float* __restrict__ b, 
 // FP64 near-source initial values: sqrt(dx^2+dy^2+dz^2) * f * h at the 8
 // nodes around each source (scripts/gene_obs.jl:44-51, order ceil/floor).
 template <class T>
-__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields, int fixed) {
+__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields, int fixed,
+                           unsigned long long* cost) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
+  cost[s] = 0;  // bricks swept by this evaluation's sweeps, for the next one's order
   SolveDev& sd = solves[s];
   const FieldDev<T>& fd = fields[sd.field];
   const int xs[2] = {sd.xc, sd.xf}, ys[2] = {sd.yc, sd.yf}, zs[2] = {sd.zc, sd.zf};
@@ -138,6 +140,7 @@ struct BatchPlan {
   DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
   DevBuf d_gdense;  // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
   DevBuf d_mis_scratch;  // seed merge arrays when they exceed shared memory
+  DevBuf d_cost, d_chunk_off, d_chunk_cnt;  // per-solve cost; chunk slices of d_order
   int64_t mis_stride = 0;
   int64_t snap_stride = 0;
   std::vector<adt_solve_status> h_status;
@@ -462,6 +465,20 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       for (int f = 0; f < n_fields; ++f) uo.insert(uo.end(), ch.field_uoff[f].begin(), ch.field_uoff[f].end());
     }
     ADT_CUDA(cudaMemcpy(P->d_order.p, ord.data(), ord.size() * 4, cudaMemcpyHostToDevice));
+    std::vector<long long> coff;
+    std::vector<int> ccnt;
+    for (auto& ch : P->chunks) {
+      coff.push_back((long long)ch.dev_order_off);
+      ccnt.push_back(ch.count);
+    }
+    R_(P->d_chunk_off, coff.size() * sizeof(long long));
+    R_(P->d_chunk_cnt, ccnt.size() * sizeof(int));
+    R_(P->d_cost, (size_t)n_solves * sizeof(unsigned long long));
+    ADT_CUDA(cudaMemcpy(P->d_chunk_off.p, coff.data(), coff.size() * sizeof(long long),
+                        cudaMemcpyHostToDevice));
+    ADT_CUDA(cudaMemcpy(P->d_chunk_cnt.p, ccnt.data(), ccnt.size() * sizeof(int),
+                        cudaMemcpyHostToDevice));
+    ADT_CUDA(cudaMemset(P->d_cost.p, 0, (size_t)n_solves * sizeof(unsigned long long)));
     if (!uo.empty()) ADT_CUDA(cudaMemcpy(P->d_uoff.p, uo.data(), uo.size() * 8, cudaMemcpyHostToDevice));
   }
   // launch shapes: warp groups (one solve each) per CTA, as many as fit
@@ -529,6 +546,7 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.next = P.d_next.as<int>() + which_counter;
   A.status = P.d_status.as<adt_solve_status>();
   A.counters = P.d_counters.as<unsigned long long>();
+  A.cost = P.d_cost.as<unsigned long long>();
   A.tol = P.opts.tol;
   A.max_iter = P.opts.max_iter;
   A.adj_max_iter = P.opts.adj_max_iter;
@@ -552,7 +570,8 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
                                                            P.geoms[f].ncell);
   k_src_init<T><<<(P.ns + 127) / 128, 128, 0, st>>>(P.d_solves.as<SolveDev>(), P.ns,
                                                      P.d_fields.as<FieldDev<T>>(),
-                                                     P.src_fixed ? 1 : 0);
+                                                     P.src_fixed ? 1 : 0,
+                                                     P.d_cost.as<unsigned long long>());
   ADT_CUDA(cudaMemsetAsync(P.d_grad.p, 0, P.ncell_total * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_next.p, 0, 2 * P.chunks.size() * 4, st));
@@ -600,6 +619,9 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
     }
   }
   k_misfit_sum<<<1, 32, 0, st>>>(P.d_smis.as<double>(), P.ns, P.d_mis.as<double>());
+  k_order_by_cost<<<(int)P.chunks.size(), 256, 0, st>>>(
+      P.d_order.as<int>(), P.d_chunk_off.as<long long>(), P.d_chunk_cnt.as<int>(),
+      P.d_cost.as<unsigned long long>());
   ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * P.chunks.size() + 1], st, evf));
   ADT_CUDA(cudaGetLastError());
   return ADT_OK;

@@ -72,6 +72,7 @@ struct BatchArgs {
   int* next;                // work counter
   adt_solve_status* status; // per global solve
   unsigned long long* counters;  // [0] fwd cell updates [1] fwd bricks [2] adj updates [3] adj bricks
+  unsigned long long* cost;  // per solve: bricks swept in this evaluation (orders the next one)
   double tol;
   int max_iter;
   int adj_max_iter;
@@ -316,6 +317,7 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
     const FieldDev<T> fd = A.fields[sd.field];
     const Geom g = fd.g;
     const T h = (T)fd.h;
+    const unsigned long long brk0 = cnt_brk;
     T* u = A.u + sd.u_off;
     const int nb = g.nbx * g.nby * g.nbz;
     int* mod = c.smeta ? c.smeta : A.meta + sd.meta_off;
@@ -417,6 +419,7 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
         break;
       }
     }
+    if (lane == 0 && cnt_brk > brk0) atomicAdd(&A.cost[sd.gidx], cnt_brk - brk0);
     if (c.gw == 0 && lane == 0) {
       adt_solve_status& st = A.status[sd.gidx];
       st.iters = conv ? it + 1 : it;
@@ -718,6 +721,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     if (q < 0) break;
     const int gsol = A.order[q];
     const SolveDev& sd = A.solves[gsol];
+    const unsigned long long brk0 = cnt_brk;
     const FieldDev<T> fd = A.fields[sd.field];
     const Geom g = fd.g;
     const T* u = A.u + sd.u_off;
@@ -857,6 +861,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     }
     if (A.gdense)  // leave the dense seed field all zero for the next evaluation
       for (int e = c.gw * 32 + lane; e < ns; e += c.gthreads) A.gdense[sd.u_off + sidx[e]] = T(0);
+    if (lane == 0 && cnt_brk > brk0) atomicAdd(&A.cost[sd.gidx], cnt_brk - brk0);
     if (c.gw == 0 && lane == 0) {
       adt_solve_status& st = A.status[sd.gidx];
       st.adj_iters = conv ? it + 1 : it;
@@ -886,6 +891,56 @@ __global__ void k_batch_grad(const T* __restrict__ lam, const int64_t* __restric
     }
     grad[c] = G;
   }
+}
+
+// Order each chunk's solves for the next evaluation by this evaluation's
+// cost (bricks swept, forward + adjoint), most expensive first, ties by solve
+// index.  With the persistent kernels' round-robin first assignment and
+// work counter, that is longest-first scheduling: the expensive solves start
+// first and share an SM with cheap ones.  Only the schedule changes; every
+// sum over solves keeps its own fixed order, so results do not.  One CTA per
+// chunk; chunks of more than ORDER_MAX solves keep their order.
+constexpr int ORDER_MAX = 4096;
+
+__global__ void k_order_by_cost(int* order, const long long* chunk_off, const int* chunk_cnt,
+                                const unsigned long long* cost) {
+  __shared__ unsigned long long key[ORDER_MAX];
+  __shared__ int idx[ORDER_MAX];
+  const int c = blockIdx.x, n = chunk_cnt[c];
+  if (n > ORDER_MAX || n < 2) return;
+  int* o = order + chunk_off[c];
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    if (i < n) {
+      idx[i] = o[i];
+      key[i] = cost[o[i]];
+    } else {
+      idx[i] = INT_MAX;
+      key[i] = 0;
+    }
+  }
+  __syncthreads();
+  // bitonic sort: cost descending, then index ascending
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int p = i ^ j;
+        if (p > i) {
+          const bool before = key[i] > key[p] || (key[i] == key[p] && idx[i] < idx[p]);
+          if (before != ((i & k) == 0)) {
+            const unsigned long long tk = key[i];
+            key[i] = key[p];
+            key[p] = tk;
+            const int ti = idx[i];
+            idx[i] = idx[p];
+            idx[p] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) o[i] = idx[i];
 }
 
 }  // namespace adt
