@@ -220,9 +220,12 @@ __device__ __forceinline__ void halo_col(int c, int& ci, int& cj) {
     if (h < 8) {                // x faces
       ci = (h < 4) ? 0 : BI + 1;
       cj = (h & 3) + 1;
-    } else {                    // y faces
-      ci = ((h - 8) & 7) + 1;
-      cj = (h < 16) ? 0 : BJ + 1;
+    } else {  // y faces, the two faces of a row interleaved: consecutive columns of one
+              // staging copy then start in different bank residues (2-way instead of
+              // 4-way conflicts; all-equal residues within a face)
+      const int q = h - 8;
+      ci = (q >> 1) + 1;
+      cj = (q & 1) ? BJ + 1 : 0;
     }
   }
 }
