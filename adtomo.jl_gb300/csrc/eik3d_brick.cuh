@@ -335,25 +335,45 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   return r;
 }
 
+// Three-input minimum and maximum (one instruction each on sm_100 and later).
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Branch-free FP32 form of upd3_stable: all three candidate roots are
 // formed and the first admissible one selected, so lanes on different
-// branches do not serialise.
+// branches do not serialise.  Arranged for a short dependency path from ax
+// and ay, which arrive last (other lanes' results of the previous step):
+// - the sort uses three-input min/max;
+// - the three-axis root (u - ax)^2 + (u - ay)^2 + (u - az)^2 = F^2 is
+//   symmetric in the three values, so it is formed relative to az (this
+//   lane's own, available early) instead of the sorted minimum:
+//   u = az + (bx + by + sqrt(3F^2 - bx^2 - by^2 - (bx - by)^2)) / 3 with
+//   b = a - az; it is only selected when every value is finite;
+// - the two-axis root x2 = lo + (d2 + r2)/2 is admissible while x2 <= hi,
+//   tested as r2 <= 2 d3 - d2 (the two roots agree on that boundary).
 __device__ __forceinline__ float upd3_f32(float ax, float ay, float az, float fh) {
-  const float lo = fminf(fminf(ax, ay), az);
-  const float hi = fmaxf(fmaxf(ax, ay), az);
-  const float mid = fmaxf(fminf(ax, ay), fminf(fmaxf(ax, ay), az));
+  const float lo = fmin3f(ax, ay, az);
+  const float hi = fmax3f(ax, ay, az);
+  const float mid = fmin3f(fmaxf(ax, ay), fmaxf(ax, az), fmaxf(ay, az));
   const float F2 = fh * fh;
   const float d2 = mid - lo;
   const float d3 = hi - lo;
   const float x1 = lo + fh;
   const float r2 = sqrt_approx(fmaxf(fmaf(-d2, d2, 2.0f * F2), 0.0f));
   const float x2 = fmaf(0.5f, d2 + r2, lo);
-  // 3F^2 - d2^2 - d3^2 - (d3 - d2)^2 = 3F^2 - 2 (d2 (d2 - d3) + d3^2): two
-  // dependent operations fewer than the sum of three squares
-  const float q = fmaf(d2, d2 - d3, d3 * d3);
-  const float r3 = sqrt_approx(fmaxf(fmaf(-2.0f, q, 3.0f * F2), 0.0f));
-  const float x3 = fmaf(d2 + d3 + r3, 1.0f / 3.0f, lo);
-  return (x1 <= mid) ? x1 : ((x2 <= hi) ? x2 : x3);
+  const float bx = ax - az, by = ay - az, bxy = ax - ay;
+  const float disc = fmaf(-bxy, bxy, fmaf(-by, by, fmaf(-bx, bx, 3.0f * F2)));
+  const float r3 = sqrt_approx(fmaxf(disc, 0.0f));
+  const float x3 = fmaf(bx + by + r3, 1.0f / 3.0f, az);
+  return (x1 <= mid) ? x1 : ((r2 <= fmaf(2.0f, d3, -d2)) ? x2 : x3);
 }
 
 // Shared-memory accesses with a 32-bit shared-window address and a
@@ -495,15 +515,18 @@ __device__ __forceinline__ float rcp_approx(float x) {
 
 // Per-cell constants of one FP32 adjoint update, formed one step ahead.
 // The user terms w_q lambda_q (w_q = u_q - u_c for a user q, else 0) are
-// summed in one fixed order whatever the sweep direction:
-//   acc = (P_x + P_y) + P_z,  P_a = fma(w_{a+}, lambda_{a+}, w_{a-} lambda_{a-}),
+// combined in one fixed order whatever the sweep direction:
+//   lambda = fma(P_x + P_y, c2, fma(P_z, c2, c0)),
+//   P_a = fma(w_{a+}, lambda_{a+}, w_{a-} lambda_{a-}),
 // so a cell evaluates to the same bits in every ordering and the sweeps
 // reach an exact fixed point (an order that followed the sweep would make
 // the orderings disagree in the last bit and never settle).  Per axis one
 // lambda is new in the sweep (the upstream neighbour) and one is old: when
 // the new one is the minus neighbour, P = fma(a, b, w_u lambda_u) with
 // (a, b) = (w_d, lambda_d); when it is the plus neighbour, P = fma(w_u,
-// lambda_u, a) with a = w_d lambda_d.  lambda = fma(acc, c2, c0).
+// lambda_u, a) with a = w_d lambda_d.  The z term is this lane's own and
+// is folded into the constant first, which keeps it off the path from the
+// other lanes' values.
 struct AdjCellF32 {
   float wx, ax, bx, wy, ay, by, wz, az, bz;
   float c2, c0;
@@ -603,10 +626,11 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
     const float n_uzd = lds<2 * DZ>(ua);
     const float n_lxd = lds<DZ + XD>(la), n_lyd = lds<DZ + YD>(la);
     const float n_lzd = lds<2 * DZ>(la);
-    const float acc = (adj_pair<SI>(cur.wx, lxu, cur.ax, cur.bx) +
-                       adj_pair<SJ>(cur.wy, lyu, cur.ay, cur.by)) +
-                      adj_pair<SKD>(cur.wz, lzu, cur.az, cur.bz);
-    const float lam = fmaf(acc, cur.c2, cur.c0);
+    // lambda = (P_x + P_y) c2 + (P_z c2 + c0): P_z is this lane's own (early)
+    const float pz = fmaf(adj_pair<SKD>(cur.wz, lzu, cur.az, cur.bz), cur.c2, cur.c0);
+    const float pxy = adj_pair<SI>(cur.wx, lxu, cur.ax, cur.bx) +
+                      adj_pair<SJ>(cur.wy, lyu, cur.ay, cur.by);
+    const float lam = fmaf(pxy, cur.c2, pz);
     const bool wr = cur.wrok && (lam != lold);
     sts_if(wr, la, lam);
     changed |= wr;
