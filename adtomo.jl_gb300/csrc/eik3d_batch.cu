@@ -178,6 +178,8 @@ void batch_opts_default(adt_batch_opts* o) {
   o->warps = 0;
   o->groups = 0;
   o->use_graph = 1;
+  o->wake_tol = 0.0;
+  o->adj_wake_tol = 0.0;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -261,6 +263,9 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     return set_error(ADT_EINVAL, "batch: ref_compat needs ADT_F64");
   if (o.max_iter < 1 || o.adj_max_iter < 1 || !(o.tol >= 0.0))
     return set_error(ADT_EINVAL, "batch: bad iteration caps or tolerance");
+  if (!(o.wake_tol >= 0.0) || !std::isfinite(o.wake_tol) || !(o.adj_wake_tol >= 0.0) ||
+      !std::isfinite(o.adj_wake_tol))
+    return set_error(ADT_EINVAL, "batch: wake_tol and adj_wake_tol must be finite and >= 0");
   if (o.bk != 0 && o.bk != 16 && o.bk != 32 && o.bk != 64)
     return set_error(ADT_EINVAL, "batch: bk must be 0, 16, 32 or 64");
   auto P = std::make_unique<BatchPlan>();
@@ -548,6 +553,8 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.counters = P.d_counters.as<unsigned long long>();
   A.cost = P.d_cost.as<unsigned long long>();
   A.tol = P.opts.tol;
+  A.wake = P.f64 ? 0.0f : (float)P.opts.wake_tol;
+  A.adj_wake = P.f64 ? 0.0f : (float)P.opts.adj_wake_tol;
   A.max_iter = P.opts.max_iter;
   A.adj_max_iter = P.opts.adj_max_iter;
   A.ref_compat = P.opts.ref_compat;

@@ -74,6 +74,8 @@ struct BatchArgs {
   unsigned long long* counters;  // [0] fwd cell updates [1] fwd bricks [2] adj updates [3] adj bricks
   unsigned long long* cost;  // per solve: bricks swept in this evaluation (orders the next one)
   double tol;
+  float wake;               // FP32 forward: decrease at or below which a brick wakes no one
+  float adj_wake;           // FP32 adjoint: relative change at or below which it wakes no one
   int max_iter;
   int adj_max_iter;
   int ref_compat;
@@ -378,8 +380,13 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
               cp_async_wait_all();
               __syncwarp();
               const bool nr = use_near && box.hits(p);
-              ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, md);
+              float mbb = 0.0f;  // this brick's largest decrease (per lane)
+              ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, mbb);
+              md = fmaxf(md, mbb);
               if (ch) store_interior_f32_vec<BK>(S, u, g, p, CS, lane);
+              // the brick's own cells keep every decrease; only a brick that moved by
+              // more than `wake` marks itself and its neighbours for the next sweeps
+              if (ch && A.wake > 0.0f) ch = __any_sync(0xffffffffu, mbb > A.wake);
             } else {
               load_halo_tile<T, BK>(S, u, g, p, CS, lane);
               load_interior<T, BK>(F, fd.f, g, p, CS, lane);
@@ -690,16 +697,16 @@ template <int BK>
 __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const uint16_t* C,
                                                  const float* gcell, const Geom& g,
                                                  const BrickPos& p, int si, int sj, int sk,
-                                                 int lane) {
+                                                 int lane, float eps, bool& sig) {
   switch ((si < 0) | ((sj < 0) << 1) | ((sk < 0) << 2)) {
-    case 0: return sweep_brick_adj_f32<BK, 1, 1, 1>(U, L, C, gcell, g, p, lane);
-    case 1: return sweep_brick_adj_f32<BK, -1, 1, 1>(U, L, C, gcell, g, p, lane);
-    case 2: return sweep_brick_adj_f32<BK, 1, -1, 1>(U, L, C, gcell, g, p, lane);
-    case 3: return sweep_brick_adj_f32<BK, -1, -1, 1>(U, L, C, gcell, g, p, lane);
-    case 4: return sweep_brick_adj_f32<BK, 1, 1, -1>(U, L, C, gcell, g, p, lane);
-    case 5: return sweep_brick_adj_f32<BK, -1, 1, -1>(U, L, C, gcell, g, p, lane);
-    case 6: return sweep_brick_adj_f32<BK, 1, -1, -1>(U, L, C, gcell, g, p, lane);
-    default: return sweep_brick_adj_f32<BK, -1, -1, -1>(U, L, C, gcell, g, p, lane);
+    case 0: return sweep_brick_adj_f32<BK, 1, 1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 1: return sweep_brick_adj_f32<BK, -1, 1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 2: return sweep_brick_adj_f32<BK, 1, -1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 3: return sweep_brick_adj_f32<BK, -1, -1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 4: return sweep_brick_adj_f32<BK, 1, 1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 5: return sweep_brick_adj_f32<BK, -1, 1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 6: return sweep_brick_adj_f32<BK, 1, -1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
+    default: return sweep_brick_adj_f32<BK, -1, -1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
   }
 }
 
@@ -824,8 +831,11 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
               load_codes_vec<BK>(C, code, g, p, CS, lane);
               cp_async_wait_all();
               __syncwarp();
-              ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane);
+              bool sig;
+              ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane,
+                                        A.adj_wake, sig);
               if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
+              ch = sig;  // only a significant change wakes neighbours and extends the solve
             } else {
               load_halo_tile<T, BK>(U, u, g, p, CS, lane);
               load_halo_tile<T, BK>(L, lam, g, p, CS, lane);

@@ -367,7 +367,8 @@ __device__ __forceinline__ float upd3_f32(float ax, float ay, float az, float fh
   const float d2 = mid - lo;
   const float d3 = hi - lo;
   const float x1 = lo + fh;
-  const float r2 = sqrt_approx(fmaxf(fmaf(-d2, d2, 2.0f * F2), 0.0f));
+  // 2F^2 - d2^2 < 0 only when d2 > F, where x1 <= mid selects x1: no clamp
+  const float r2 = sqrt_approx(fmaf(-d2, d2, 2.0f * F2));
   const float x2 = fmaf(0.5f, d2 + r2, lo);
   const float bx = ax - az, by = ay - az, bxy = ax - ay;
   const float disc = fmaf(-bxy, bxy, fmaf(-by, by, fmaf(-bx, bx, 3.0f * F2)));
@@ -448,10 +449,10 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
       un = (float)upd3_stable<double>((double)ax, (double)ay, (double)az, (double)fc * hd);
     else
       un = upd3_f32(ax, ay, az, fc * h);
-    const float d = act ? uo - un : 0.0f;
-    sts_if(d > 0.0f, a, un);
-    mb = fmaxf(mb, d);
-    prev = d > 0.0f ? un : uo;
+    const bool wr = act && (un < uo);
+    sts_if(wr, a, un);
+    mb = fmaxf(mb, act ? uo - un : 0.0f);
+    prev = wr ? un : uo;
     uo = dn;
     dn = n_dn;
     xd = n_xd;
@@ -585,10 +586,16 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
 // dependency path is two shared loads, at most five FMA-pipe operations and
 // the store.  U and L
 // share one tile layout; SI, SJ, SKD: sweep directions.
+//
+// Returns whether any lambda of the brick changed (the tile must be written
+// back); `sig` tells whether one changed by more than eps relative
+// (|new - old| > eps |new|), which is what wakes the brick's neighbours.
+// With eps = 0 the two are the same.
 template <int BK, int SI, int SJ, int SKD>
 __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, const uint16_t* C,
                                                     const float* gcell, const Geom& g,
-                                                    const BrickPos& p, int lane) {
+                                                    const BrickPos& p, int lane, float eps,
+                                                    bool& sig) {
   constexpr int RS = tile_row_stride(BK);
   constexpr int IRS = itile_row_stride(BK);
   constexpr int CS = tile_col_stride(BK, SJ == SKD);
@@ -615,6 +622,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
       ldsu16(ca), uc, lds<XU>(ua), lds<XD>(ua), lds<YU>(ua), lds<YD>(ua), lds<-DZ>(ua), uzd,
       lds<XD>(la), lds<YD>(la), lzd, (unsigned)(-s) < (unsigned)nk, gcol - SKD * s, gcell);
   bool changed = false;
+  float rmax = -1.0f;  // largest |new - old| - eps |new| over this lane's writes
   const int nsteps = p.nk + SKEW;
 #pragma unroll 4
   for (int tau = 0; tau < nsteps; ++tau) {
@@ -634,6 +642,8 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
     const bool wr = cur.wrok && (lam != lold);
     sts_if(wr, la, lam);
     changed |= wr;
+    const float rel = fmaf(-eps, fabsf(lam), fabsf(lam - lold));
+    rmax = wr ? fmaxf(rmax, rel) : rmax;
     lzu = wr ? lam : lold;
     const int kn = tau + 1 - s;
     cur = adj_cell_f32<SI, SJ, SKD>(n_code, uzd, n_uxu, n_uxd, n_uyu, n_uyd, uc, n_uzd, n_lxd,
@@ -648,7 +658,9 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
     ca += DC;
     __syncwarp();
   }
-  return __any_sync(0xffffffffu, changed);
+  const bool any = __any_sync(0xffffffffu, changed);
+  sig = eps > 0.0f ? __any_sync(0xffffffffu, rmax > 0.0f) : any;
+  return any;
 }
 
 // Adjoint sweep of one staged brick: lambda_c = (g_c + sum_users 2 (u_r - u_c)

@@ -188,7 +188,8 @@ def run_ours(args, rank, world):
     f, f_obs, sta, src, w = workload()
     sf = np.zeros(N_EVENTS, np.int32)
     B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
-                  warps=args.warps, groups=args.groups)
+                  warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
+                  adj_wake_tol=args.adj_wake_tol)
     # observed times from the +2% noise model (setup, untimed)
     B.upload([f_obs], np.full(N_EVENTS * N_STA, 1.0), w)
     B.run_resident()
@@ -229,6 +230,16 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
     clocks = clk.summary()
+    vs_exact = None
+    if rank == 0 and (args.wake_tol > 0 or args.adj_wake_tol > 0):
+        # untimed: the same evaluation with exact brick skipping, as the yardstick of
+        # what the wake tolerances changed
+        E = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6)
+        _, tp_x, g_x, _ = E.run([f], t_obs, w)
+        E.close()
+        vs_exact = {"t_pred_max_rel": float(np.max(np.abs(tp - tp_x) / np.abs(tp_x))),
+                    "grad_rel_l2": float(np.linalg.norm(grads[0] - g_x[0]) /
+                                         np.linalg.norm(g_x[0]))}
     t = torch.tensor([ms, e2e_s * 1000.0], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -284,7 +295,9 @@ def run_ours(args, rank, world):
                    else "fixed",
                    "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
-                   "adj_iters_mean": float(np.mean([s.adj_iters for s in status]))},
+                   "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
+                   "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
+                   "vs_exact_skipping": vs_exact},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -344,7 +357,8 @@ def run_large(args):
     import adtomo_gb300 as A
     rng = np.random.default_rng(SEED)
     fields, stations, slow, sf, src, chunk, desc = large_workload(args.workload, rng)
-    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, chunk=chunk)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, chunk=chunk,
+                  wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol)
     n_obs = sum(len(stations[f]) for f in sf)
     B.upload(slow, np.full(n_obs, 1.0), np.ones(n_obs))
     B.run_resident()
@@ -371,6 +385,7 @@ def run_large(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "solves": int(len(sf)), "chunk": chunk,
+                   "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
                    "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
                    "cell_updates_per_s": (st.fwd_cell_updates + st.adj_cell_updates) /
                    (ms_step / 1000.0),
@@ -452,6 +467,11 @@ def main():
     ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5", "inversion"],
                     help="c3 (default): the headline; c4, c5: secondary lines for the larger "
                          "configurations")
+    ap.add_argument("--wake-tol", type=float, default=1e-6,
+                    help="forward: a brick that moved by at most this (s) wakes no neighbour "
+                         "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
+    ap.add_argument("--adj-wake-tol", type=float, default=1e-5,
+                    help="adjoint: the same for relative changes (default 1e-5; 0 = exact)")
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,

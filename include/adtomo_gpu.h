@@ -167,6 +167,13 @@ typedef struct adt_batch_opts {
   int32_t warps;        /* warps per solve (one warp group per solve): 0 = default */
   int32_t groups;       /* solves resident per CTA (warp groups): 0 = as many as fit */
   int32_t use_graph;    /* 1 (default): replay the evaluation as a CUDA graph */
+  double wake_tol;      /* FP32 forward: a brick whose largest travel-time decrease in a
+                           sweep is at most wake_tol (s) does not wake its neighbours;
+                           0 (default) = exact skipping.  Ignored in FP64. */
+  double adj_wake_tol;  /* FP32 adjoint: a brick whose largest relative adjoint change
+                           |new - old| / |new| in a sweep is at most adj_wake_tol wakes
+                           no neighbour and does not extend the solve; 0 (default) =
+                           exact (iterate until nothing changes).  Ignored in FP64. */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;

@@ -241,6 +241,39 @@ def test_batch_fp32_accuracy_against_fp64():
     B.close()
 
 
+def test_batch_fp32_wake_tolerances_against_fp64():
+    """Bricks that moved by at most wake_tol (forward, seconds) or adj_wake_tol
+    (adjoint, relative) wake no neighbours: results stay within the FP32
+    tolerances of the converged FP64 oracle, and stay independent of the
+    launch shape."""
+    rng = np.random.default_rng(8)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(40, 36, 24, 0.5), (24, 24, 48, 0.5)], 8, 12)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    first = None
+    for kw in ({"wake_tol": 1e-6, "adj_wake_tol": 1e-5}, {"wake_tol": 1e-6, "adj_wake_tol": 1e-5,
+                                                          "warps": 3, "groups": 2},
+               {"wake_tol": 1e-5, "adj_wake_tol": 1e-4}):
+        B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, **kw)
+        mis, tp, grads, st = B.run(slow, t_obs, w)
+        # tolerances: travel times 1e-4 relative, gradient 1e-3 relative (L2)
+        assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4, kw
+        assert abs(mis - mo) <= 1e-3 * mo, kw
+        for g, r in zip(grads, go):
+            assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r), kw
+        assert all(s.converged and s.adj_converged for s in st), kw
+        if first is None:
+            first = (tp, grads[0])
+        elif "warps" in kw:
+            assert np.array_equal(tp, first[0]) and np.array_equal(grads[0], first[1])
+        B.close()
+    with pytest.raises(A.AdtError):
+        A.Batch3D(fields, stations, sf, src, wake_tol=-1.0)
+    with pytest.raises(A.AdtError):
+        A.Batch3D(fields, stations, sf, src, adj_wake_tol=float("nan"))
+
+
 def test_batch_chunking_and_graph_do_not_change_results():
     rng = np.random.default_rng(9)
     fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 7, 6)
