@@ -458,8 +458,8 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
     xd = n_xd;
     yd = n_yd;
     fc = n_fc;
-    a += DZ;
-    fa += DZ;
+    a += (uint32_t)DZ;  // wraps for a negative step
+    fa += (uint32_t)DZ;
     __syncwarp();
   }
   maxdec = fmaxf(maxdec, mb);
@@ -628,7 +628,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
   for (int tau = 0; tau < nsteps; ++tau) {
     const float lxu = lds<XU>(la), lyu = lds<YU>(la);
     // next cell's operands
-    const uint32_t n_code = ldsu16(ca + DC);
+    const uint32_t n_code = ldsu16(ca + (uint32_t)DC);
     const float n_uxu = lds<DZ + XU>(ua), n_uxd = lds<DZ + XD>(ua);
     const float n_uyu = lds<DZ + YU>(ua), n_uyd = lds<DZ + YD>(ua);
     const float n_uzd = lds<2 * DZ>(ua);
@@ -653,9 +653,9 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
     uzd = n_uzd;
     lold = lzd;
     lzd = n_lzd;
-    ua += DZ;
-    la += DZ;
-    ca += DC;
+    ua += (uint32_t)DZ;  // wraps for a negative step
+    la += (uint32_t)DZ;
+    ca += (uint32_t)DC;
     __syncwarp();
   }
   const bool any = __any_sync(0xffffffffu, changed);
