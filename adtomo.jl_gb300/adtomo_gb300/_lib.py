@@ -75,6 +75,7 @@ SIGNATURES = {
                                                   _P]),
     "adt_eikonal_three_d_device_noalloc": (C.c_int, [_P, _P, _D, _I64, _I64, _I64, _D, C.c_int,
                                                      _P, _P, _P]),
+    "adt_abi_struct_sizes": (C.c_int, [_P, _I32]),
     "adt_batch_opts_default": (None, [_P]),
     "adt_batch_create": (C.c_int, [_P, _I32, _P, _P, _P, _P, _I32, _P, _P, _P]),
     "adt_batch_destroy": (C.c_int, [_P]),
@@ -108,6 +109,13 @@ def lib(build_if_missing: bool = True):
                 fn = getattr(L, name)
                 fn.restype = res
                 fn.argtypes = args
+            sizes = (C.c_int64 * 3)()
+            L.adt_abi_struct_sizes(sizes, 3)
+            mirrors = (SolveStatus, BatchOpts, BatchStats)
+            if tuple(sizes) != tuple(C.sizeof(m) for m in mirrors):
+                raise AdtError(-1, f"struct sizes of {LIB_PATH} {tuple(sizes)} differ "
+                                           f"from the ctypes mirrors "
+                                           f"{tuple(C.sizeof(m) for m in mirrors)}")
             _lib = L
     return _lib
 

@@ -97,6 +97,13 @@ const char* adt_last_error(void) { return g_err; }
 
 const char* adt_version(void) { return "adtomo-gb300 0.1 (sm_103a)"; }
 
+int adt_abi_struct_sizes(int64_t* out, int n) {
+  const int64_t sz[3] = {(int64_t)sizeof(adt_solve_status), (int64_t)sizeof(adt_batch_opts),
+                         (int64_t)sizeof(adt_batch_stats)};
+  for (int i = 0; out && i < n && i < 3; ++i) out[i] = sz[i];
+  return 3;
+}
+
 int adt_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {

@@ -55,6 +55,11 @@ const char* adt_last_error(void);
 const char* adt_version(void);
 /* Number of usable devices (0 when none); never fails. */
 int adt_device_count(void);
+/* Sizes of the structs this header defines, for bindings to check their
+ * mirrors against: out[0] = sizeof(adt_solve_status), out[1] =
+ * sizeof(adt_batch_opts), out[2] = sizeof(adt_batch_stats).  Writes at most
+ * n entries and returns the number of structs (3); never fails. */
+int adt_abi_struct_sizes(int64_t* out, int n);
 
 /* ------------------------------------------------------------------------
  * 2D op: replaces Eikonal (Eikonal.cpp:20-46, Compute :74-127).

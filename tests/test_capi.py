@@ -28,6 +28,14 @@ def test_library_exports_every_declared_symbol():
     assert set(syms) == set(_lib.SIGNATURES), "ctypes signatures must cover the header exactly"
 
 
+def test_struct_mirrors_match_the_library():
+    import ctypes as C
+    sizes = (C.c_int64 * 3)()
+    assert A.lib().adt_abi_struct_sizes(sizes, 3) == 3
+    assert tuple(sizes) == (C.sizeof(_lib.SolveStatus), C.sizeof(_lib.BatchOpts),
+                            C.sizeof(_lib.BatchStats))
+
+
 def test_version_and_device_count_do_not_fail():
     L = A.lib()
     assert b"sm_103a" in L.adt_version()
