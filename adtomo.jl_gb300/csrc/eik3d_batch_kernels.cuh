@@ -197,15 +197,26 @@ __device__ __forceinline__ GroupCtx group_ctx(const BatchArgs<T>& A, unsigned ch
 }
 
 // Take the next solve for this group (or -1 when the queue is empty).  The
-// first solve of every group is assigned round-robin across CTAs (group g of
-// CTA b takes g * gridDim.x + b), so every SM gets a solve before any SM
-// gets a second; later solves come from the shared counter.
+// first solve of every group is assigned statically, so every SM gets a
+// solve before any SM gets a second: group 0 of CTA b takes solve b, and the
+// solves of each later round go to the CTAs whose earlier solves are the
+// lightest (solves are ordered heaviest first), the heaviest of the round to
+// the last CTA.  The heaviest solves then run alone on their SM and the
+// lighter ones share, which shortens the longest SM.  Later solves come from
+// the shared counter.
 template <class T>
 __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx& c, bool& first) {
   int q;
   if (first) {
     first = false;
-    q = c.grp * (int)gridDim.x + (int)blockIdx.x;
+    const int C = (int)gridDim.x, b = (int)blockIdx.x;
+    if (c.grp == 0) {
+      q = b;
+    } else {
+      const int r0 = c.grp * C;                          // first solve of this round
+      const int cnt = min(C, max(A.n_solves - r0, 0));   // solves in this round
+      q = b >= C - cnt ? r0 + (C - 1 - b) : A.n_solves;  // none for the heavier CTAs
+    }
   } else {
     if (c.gw == 0 && c.lane == 0) c.gs->q = atomicAdd(A.next, 1) + c.G * (int)gridDim.x;
     group_sync(c.grp, c.gthreads);
