@@ -160,7 +160,9 @@ class Batch3D:
             pass
 
     def _inputs(self, slowness, t_obs, weight):
-        slow = np.concatenate([_f64(s, "slowness").ravel() for s in slowness])
+        # one field: the caller's buffer itself (no host copy, so pinned memory stays pinned)
+        slow = (_f64(slowness[0], "slowness").ravel() if len(slowness) == 1 else
+                np.concatenate([_f64(s, "slowness").ravel() for s in slowness]))
         if slow.size != sum(self.ncell):
             raise AdtError(-1, "slowness size does not match the fields")
         t_obs = _f64(t_obs, "t_obs").ravel()
@@ -176,12 +178,21 @@ class Batch3D:
             off += nc
         return out
 
-    def run(self, slowness, t_obs, weight):
-        """One evaluation end to end through adt_batch_run (host buffers)."""
+    def run(self, slowness, t_obs, weight, out=None):
+        """One evaluation end to end through adt_batch_run (host buffers).
+        out: optional (t_pred, grad) float64 buffers of n_obs and total-cell
+        entries to write into (e.g. pinned memory) instead of new arrays."""
         slow, t_obs, weight = self._inputs(slowness, t_obs, weight)
         mis = C.c_double(0)
-        tp = np.empty(self.n_obs)
-        gr = np.empty(sum(self.ncell))
+        if out is None:
+            tp, gr = np.empty(self.n_obs), np.empty(sum(self.ncell))
+        else:
+            tp, gr = out
+            if (tp.dtype != np.float64 or gr.dtype != np.float64 or not tp.flags.c_contiguous or
+                    not gr.flags.c_contiguous or tp.size != self.n_obs or
+                    gr.size != sum(self.ncell)):
+                raise AdtError(-1, "out must be contiguous float64 (t_pred, grad) buffers "
+                                   f"of {self.n_obs} and {sum(self.ncell)} entries")
         st = (SolveStatus * self.n_solves)()
         check(self._L.adt_batch_run(self._h, _ptr(slow), _ptr(t_obs), _ptr(weight), C.byref(mis),
                                     _ptr(tp), _ptr(gr), st))

@@ -625,6 +625,11 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
       ADT_CUDA(cudaLaunchKernel(P.ks.grad, dim3(grid1d(nc)), dim3(256), args, 0, st));
     }
   }
+  if (!P.f64)
+    for (int f = 0; f < P.nf; ++f)
+      k_grad_scale<<<grid1d(P.geoms[f].ncell), 256, 0, st>>>(
+          P.d_slow64.as<double>() + P.cell_off[f], P.h[f], P.geoms[f].ncell,
+          P.d_grad.as<double>() + P.cell_off[f]);
   k_misfit_sum<<<1, 32, 0, st>>>(P.d_smis.as<double>(), P.ns, P.d_mis.as<double>());
   k_order_by_cost<<<(int)P.chunks.size(), 256, 0, st>>>(
       P.d_order.as<int>(), P.d_chunk_off.as<long long>(), P.d_chunk_cnt.as<int>(),

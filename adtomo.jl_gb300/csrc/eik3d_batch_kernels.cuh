@@ -898,27 +898,52 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
 // --------------------------------------------------------------- gradient
 // grad[c] += sum over the chunk's solves on this field (in solve order) of
 // -lambda_s[c] * (-2 f h h), in FP64 (Eikonal3D.cpp:163-166,244-246).
+// - FP64 plans form every product and add it in solve order, as the oracle's
+//   batch does (bit-identical).
+// - FP32 plans add the solves' -lambda (exact conversions, FP64 sum in solve
+//   order, carried across chunks in grad) and k_grad_scale multiplies by
+//   -2 f h h once after the last chunk: half the FP64 operations, no less
+//   accurate, and the same bits however the solves are chunked.
+// Loads are issued eight solves ahead of the adds.
 template <class T>
 __global__ void k_batch_grad(const T* __restrict__ lam, const int64_t* __restrict__ u_off,
                              int n_solves, const double* __restrict__ f64, double h, int64_t ncell,
                              double* __restrict__ grad) {
+  constexpr int U = 8;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
        c += (int64_t)gridDim.x * blockDim.x) {
-    const double rhs = __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f64[c]), h), h);
+    const double rhs =
+        sizeof(T) == 4 ? 0.0 : __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f64[c]), h), h);
     double G = grad[c];
-    for (int s = 0; s < n_solves; ++s) {
+    int s = 0;
+    for (; s + U <= n_solves; s += U) {
+      double l[U];
+#pragma unroll
+      for (int q = 0; q < U; ++q) l[q] = (double)lam[u_off[s + q] + c];
+#pragma unroll
+      for (int q = 0; q < U; ++q)
+        G = sizeof(T) == 4 ? __dadd_rn(G, -l[q]) : __dadd_rn(G, __dmul_rn(-l[q], rhs));
+    }
+    for (; s < n_solves; ++s) {
       const double l = (double)lam[u_off[s] + c];
-      G = __dadd_rn(G, __dmul_rn(-l, rhs));
+      G = sizeof(T) == 4 ? __dadd_rn(G, -l) : __dadd_rn(G, __dmul_rn(-l, rhs));
     }
     grad[c] = G;
   }
 }
 
+// FP32 plans, after the last chunk: grad[c] = (sum of -lambda) * (-2 f h h).
+__global__ void k_grad_scale(const double* __restrict__ f64, double h, int64_t ncell,
+                             double* __restrict__ grad) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
+       c += (int64_t)gridDim.x * blockDim.x)
+    grad[c] = __dmul_rn(grad[c], __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f64[c]), h), h));
+}
+
 // Order each chunk's solves for the next evaluation by this evaluation's
 // cost (bricks swept, forward + adjoint), most expensive first, ties by solve
-// index.  With the persistent kernels' round-robin first assignment and
-// work counter, that is longest-first scheduling: the expensive solves start
-// first and share an SM with cheap ones.  Only the schedule changes; every
+// index.  With the persistent kernels' static first assignment (group_next)
+// and work counter, that is longest-first scheduling.  Only the schedule changes; every
 // sum over solves keeps its own fixed order, so results do not.  One CTA per
 // chunk; chunks of more than ORDER_MAX solves keep their order.
 constexpr int ORDER_MAX = 4096;
