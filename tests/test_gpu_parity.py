@@ -274,6 +274,22 @@ def test_batch_fp32_wake_tolerances_against_fp64():
         A.Batch3D(fields, stations, sf, src, adj_wake_tol=float("nan"))
 
 
+def test_batch_run_into_caller_buffers():
+    rng = np.random.default_rng(12)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 5, 6)
+    B = A.Batch3D(fields, stations, sf, src)
+    mis, tp, grads, _ = B.run(slow, t_obs, w)
+    out = (np.full(tp.size, np.nan), np.full(grads[0].size, np.nan))
+    mis2, tp2, grads2, _ = B.run(slow, t_obs, w, out=out)
+    assert mis2 == mis and np.array_equal(tp2, tp) and np.array_equal(grads2[0], grads[0])
+    assert np.shares_memory(tp2, out[0]) and np.shares_memory(grads2[0], out[1])
+    with pytest.raises(A.AdtError):
+        B.run(slow, t_obs, w, out=(np.empty(tp.size), np.empty(3)))
+    with pytest.raises(A.AdtError):
+        B.run(slow, t_obs, w, out=(np.empty(tp.size, np.float32), out[1]))
+    B.close()
+
+
 def test_batch_chunking_and_graph_do_not_change_results():
     rng = np.random.default_rng(9)
     fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 7, 6)
