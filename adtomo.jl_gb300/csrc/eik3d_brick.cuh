@@ -237,6 +237,21 @@ __device__ __forceinline__ void store_interior_f32_vec(const float* S, float* __
   constexpr int RS = tile_row_stride(BK);
   constexpr int CH = BK / 4;
   constexpr int PER = BI * BJ * CH / 32;
+  if constexpr (BK == 32) {
+    if (p.ni == BI && p.nj == BJ && p.nk == BK) {  // full brick: same copies, no checks
+      const int gq = lane >> 3, k = 4 * (lane & 7);
+      const int64_t nl = (int64_t)g.n * g.l;
+      float* dp = dst + ((int64_t)p.i0 * g.n + (p.j0 + gq)) * g.l + p.k0 + k;
+      const float* s = S + RS + (gq + 1) * CS + 1 + k;
+#pragma unroll
+      for (int t = 0; t < BI; ++t) {
+        const float* st = s + t * RS;
+        *reinterpret_cast<float4*>(dp) = make_float4(st[0], st[1], st[2], st[3]);
+        dp += nl;
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (int t = 0; t < PER; ++t) {
     const int e = lane + 32 * t;
@@ -282,6 +297,41 @@ __device__ __forceinline__ void load_tile_f32_async(float* S, const float* src, 
     const uint32_t dh = d + 4u * (uint32_t)(1 + p.nk);
     if (in && p.k0 + p.nk < g.l) cp_async4(dh, col + p.nk); else sts4(dh, ghost);
   }
+  if constexpr (BK == 32) {
+    if (p.i0 >= 1 && p.j0 >= 1 && p.i0 + BI + 1 <= g.m && p.j0 + BJ + 1 <= g.n && p.nk == BK) {
+      // whole halo inside the grid: the copies of the loop below (halo_col's
+      // columns, lane group gq = lane / 8 on column gq of each group of four),
+      // with per-lane bases and constant offsets instead of per-copy checks
+      const int gq = lane >> 3, k = 4 * (lane & 7);
+      const int64_t nl = (int64_t)g.n * g.l;
+      // columns 1..BJ of rows 0..BI+1 (interior rows and both x faces)
+      const float* sp = src + ((int64_t)(p.i0 - 1) * g.n + (p.j0 + gq)) * g.l + p.k0 + k;
+      const uint32_t da = s0 + 4u * (uint32_t)((gq + 1) * CS + 1 + k);
+#pragma unroll
+      for (int ci = 0; ci < BI + 2; ++ci) {
+        const uint32_t dd = da + 4u * (uint32_t)(ci * RS);
+        cp_async4(dd, sp);
+        cp_async4(dd + 4, sp + 1);
+        cp_async4(dd + 8, sp + 2);
+        cp_async4(dd + 12, sp + 3);
+        sp += nl;
+      }
+      // y faces: columns 0 and BJ+1 of rows 1..BI, interleaved as in halo_col
+      const int cib = (gq >> 1) + 1, cjb = (gq & 1) ? BJ + 1 : 0;
+      sp = src + ((int64_t)(p.i0 + cib - 1) * g.n + (p.j0 + cjb - 1)) * g.l + p.k0 + k;
+      const uint32_t db = s0 + 4u * (uint32_t)(cib * RS + cjb * CS + 1 + k);
+#pragma unroll
+      for (int r = 0; r < BI / 2; ++r) {
+        const uint32_t dd = db + 4u * (uint32_t)(2 * r * RS);
+        cp_async4(dd, sp);
+        cp_async4(dd + 4, sp + 1);
+        cp_async4(dd + 8, sp + 2);
+        cp_async4(dd + 12, sp + 3);
+        sp += 2 * nl;
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (int t = 0; t < PER; ++t) {
     const int e = lane + 32 * t;
@@ -312,6 +362,24 @@ __device__ __forceinline__ void load_interior_f32_async(float* S, const float* s
   constexpr int CH = BK / 4;
   constexpr int PER = BI * BJ * CH / 32;
   const uint32_t s0 = smem_u32(S);
+  if constexpr (BK == 32) {
+    if (p.ni == BI && p.nj == BJ && p.nk == BK) {  // full brick: same copies, no checks
+      const int gq = lane >> 3, k = 4 * (lane & 7);
+      const int64_t nl = (int64_t)g.n * g.l;
+      const float* sp = src + ((int64_t)p.i0 * g.n + (p.j0 + gq)) * g.l + p.k0 + k;
+      const uint32_t da = s0 + 4u * (uint32_t)(gq * CS + k);
+#pragma unroll
+      for (int t = 0; t < BI; ++t) {
+        const uint32_t dd = da + 4u * (uint32_t)(t * IRS);
+        cp_async4(dd, sp);
+        cp_async4(dd + 4, sp + 1);
+        cp_async4(dd + 8, sp + 2);
+        cp_async4(dd + 12, sp + 3);
+        sp += nl;
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (int t = 0; t < PER; ++t) {
     const int e = lane + 32 * t;
@@ -477,16 +545,32 @@ __device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* src,
   uint4 v[PER];
   int dst[PER];
   bool ok[PER];
+  if (BK == 32 && p.ni == BI && p.nj == BJ && p.nk == BK) {
+    // full brick: the same loads (chunk c = lane / 4 + 8 t is row 2 t + lane / 16,
+    // column (lane / 4) mod 4, cells 8 (lane mod 4) ..), one base per lane
+    const int ci = lane >> 4, cj = (lane >> 2) & 3, k = 8 * (lane & 3);
+    const int64_t nl2 = 2 * (int64_t)g.n * g.l;
+    const uint16_t* sp = src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k;
+    const int d0 = ci * IRS + cj * CS + k;
 #pragma unroll
-  for (int t = 0; t < PER; ++t) {
-    const int e = lane + 32 * t;
-    const int c = e / CH, ch = e - (e / CH) * CH;
-    const int ci = c >> 2, cj = c & 3, k = 8 * ch;
-    ok[t] = ci < p.ni && cj < p.nj && k < p.nk;
-    if (ok[t])
-      v[t] = *(reinterpret_cast<const uint4*>(
-          src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k));
-    dst[t] = ci * IRS + cj * CS + k;
+    for (int t = 0; t < PER; ++t) {
+      v[t] = *(reinterpret_cast<const uint4*>(sp));
+      sp += nl2;
+      dst[t] = d0 + 2 * t * IRS;
+      ok[t] = true;
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+      const int e = lane + 32 * t;
+      const int c = e / CH, ch = e - (e / CH) * CH;
+      const int ci = c >> 2, cj = c & 3, k = 8 * ch;
+      ok[t] = ci < p.ni && cj < p.nj && k < p.nk;
+      if (ok[t])
+        v[t] = *(reinterpret_cast<const uint4*>(
+            src + ((int64_t)(p.i0 + ci) * g.n + (p.j0 + cj)) * g.l + p.k0 + k));
+      dst[t] = ci * IRS + cj * CS + k;
+    }
   }
 #pragma unroll
   for (int t = 0; t < PER; ++t)
