@@ -708,17 +708,21 @@ template <int BK>
 __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const uint16_t* C,
                                                  const float* gcell, const Geom& g,
                                                  const BrickPos& p, int si, int sj, int sk,
-                                                 int lane, float eps, bool& sig) {
+                                                 int lane, float eps, bool seeds, bool& sig) {
+#define ADT_ADJ_CASE(SI, SJ, SK)                                                              \
+  return seeds ? sweep_brick_adj_f32<BK, SI, SJ, SK, true>(U, L, C, gcell, g, p, lane, eps, sig) \
+               : sweep_brick_adj_f32<BK, SI, SJ, SK, false>(U, L, C, gcell, g, p, lane, eps, sig)
   switch ((si < 0) | ((sj < 0) << 1) | ((sk < 0) << 2)) {
-    case 0: return sweep_brick_adj_f32<BK, 1, 1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
-    case 1: return sweep_brick_adj_f32<BK, -1, 1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
-    case 2: return sweep_brick_adj_f32<BK, 1, -1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
-    case 3: return sweep_brick_adj_f32<BK, -1, -1, 1>(U, L, C, gcell, g, p, lane, eps, sig);
-    case 4: return sweep_brick_adj_f32<BK, 1, 1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
-    case 5: return sweep_brick_adj_f32<BK, -1, 1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
-    case 6: return sweep_brick_adj_f32<BK, 1, -1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
-    default: return sweep_brick_adj_f32<BK, -1, -1, -1>(U, L, C, gcell, g, p, lane, eps, sig);
+    case 0: ADT_ADJ_CASE(1, 1, 1);
+    case 1: ADT_ADJ_CASE(-1, 1, 1);
+    case 2: ADT_ADJ_CASE(1, -1, 1);
+    case 3: ADT_ADJ_CASE(-1, -1, 1);
+    case 4: ADT_ADJ_CASE(1, 1, -1);
+    case 5: ADT_ADJ_CASE(-1, 1, -1);
+    case 6: ADT_ADJ_CASE(1, -1, -1);
+    default: ADT_ADJ_CASE(-1, -1, -1);
   }
+#undef ADT_ADJ_CASE
 }
 
 template <class T, int BK>
@@ -839,12 +843,12 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
             if (vec) {
               load_tile_f32_async<BK>(U, u, g, p, CS, lane);
               load_tile_f32_async<BK>(L, lam, g, p, CS, lane, 0.0f);
-              load_codes_vec<BK>(C, code, g, p, CS, lane);
+              const bool seeds = load_codes_vec<BK>(C, code, g, p, CS, lane);
               cp_async_wait_all();
               __syncwarp();
               bool sig;
               ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane,
-                                        A.adj_wake, sig);
+                                        A.adj_wake, seeds, sig);
               if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
               ch = sig;  // only a significant change wakes neighbours and extends the solve
             } else {

@@ -536,8 +536,9 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
 
 // Interior codes (uint16) with 16-byte vector loads: 8 codes per chunk.
 // Needs the k extent to be a multiple of 8 (16-byte aligned column segments).
+// Returns whether any code of the brick has the seed bit (warp-uniform).
 template <int BK>
-__device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* src,
+__device__ __forceinline__ bool load_codes_vec(uint16_t* S, const uint16_t* src,
                                                const Geom& g, const BrickPos& p, int CS, int lane) {
   constexpr int IRS = itile_row_stride(BK);
   constexpr int CH = BK / 8;
@@ -572,6 +573,11 @@ __device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* src,
       dst[t] = ci * IRS + cj * CS + k;
     }
   }
+  constexpr uint32_t SEED2 = (uint32_t)CODE_SEED | ((uint32_t)CODE_SEED << 16);
+  uint32_t seeds = 0;
+#pragma unroll
+  for (int t = 0; t < PER; ++t)
+    if (ok[t]) seeds |= (v[t].x | v[t].y | v[t].z | v[t].w) & SEED2;
 #pragma unroll
   for (int t = 0; t < PER; ++t)
     if (ok[t]) {
@@ -585,6 +591,7 @@ __device__ __forceinline__ void load_codes_vec(uint16_t* S, const uint16_t* src,
       d[6] = (uint16_t)(v[t].w & 0xffffu);
       d[7] = (uint16_t)(v[t].w >> 16);
     }
+  return __any_sync(0xffffffffu, seeds != 0);
 }
 
 __device__ __forceinline__ uint32_t ldsu16(uint32_t a) {
@@ -628,7 +635,7 @@ __device__ __forceinline__ float adj_pair(float w_u, float l_u, float a, float b
 // downstream along x for the sweep, likewise y and z).  Inactive terms are
 // selected away (selects, not products, so +inf ghosts never turn into NaN);
 // the adjoint tile's ghosts are 0, so their zero weights multiply zeros.
-template <int SI, int SJ, int SKD>
+template <int SI, int SJ, int SKD, bool SEEDS>
 __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, float uxu, float uxd,
                                                    float uyu, float uyd, float uzu, float uzd,
                                                    float lxd, float lyd, float lzd, bool act,
@@ -655,9 +662,13 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
   float d = fmaxf(uc - fminf(uxu, uxd), 0.0f);
   d += fmaxf(uc - fminf(uyu, uyd), 0.0f);
   d += fmaxf(uc - fminf(uzu, uzd), 0.0f);
-  const float gs = (act && (code & CODE_SEED)) ? gcell[cell] : 0.0f;
   c.c2 = rcp_approx(d);
-  c.c0 = 0.5f * gs * c.c2;
+  if constexpr (SEEDS) {
+    const float gs = (act && (code & CODE_SEED)) ? gcell[cell] : 0.0f;
+    c.c0 = 0.5f * gs * c.c2;
+  } else {
+    c.c0 = 0.0f;
+  }
   c.wrok = act && !(code & CODE_FIXED);
   return c;
 }
@@ -674,8 +685,9 @@ __device__ __forceinline__ AdjCellF32 adj_cell_f32(uint32_t code, float uc, floa
 // Returns whether any lambda of the brick changed (the tile must be written
 // back); `sig` tells whether one changed by more than eps relative
 // (|new - old| > eps |new|), which is what wakes the brick's neighbours.
-// With eps = 0 the two are the same.
-template <int BK, int SI, int SJ, int SKD>
+// With eps = 0 the two are the same.  SEEDS = false for a brick whose staged
+// codes carry no seed bit: no seed value is looked up.
+template <int BK, int SI, int SJ, int SKD, bool SEEDS>
 __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, const uint16_t* C,
                                                     const float* gcell, const Geom& g,
                                                     const BrickPos& p, int lane, float eps,
@@ -702,7 +714,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
   float uc = lds<0>(ua), uzd = lds<DZ>(ua);
   float lold = lds<0>(la), lzd = lds<DZ>(la);
   float lzu = lds<-DZ>(la);
-  AdjCellF32 cur = adj_cell_f32<SI, SJ, SKD>(
+  AdjCellF32 cur = adj_cell_f32<SI, SJ, SKD, SEEDS>(
       ldsu16(ca), uc, lds<XU>(ua), lds<XD>(ua), lds<YU>(ua), lds<YD>(ua), lds<-DZ>(ua), uzd,
       lds<XD>(la), lds<YD>(la), lzd, (unsigned)(-s) < (unsigned)nk, gcol - SKD * s, gcell);
   bool changed = false;
@@ -730,7 +742,7 @@ __device__ __forceinline__ bool sweep_brick_adj_f32(const float* U, float* L, co
     rmax = wr ? fmaxf(rmax, rel) : rmax;
     lzu = wr ? lam : lold;
     const int kn = tau + 1 - s;
-    cur = adj_cell_f32<SI, SJ, SKD>(n_code, uzd, n_uxu, n_uxd, n_uyu, n_uyd, uc, n_uzd, n_lxd,
+    cur = adj_cell_f32<SI, SJ, SKD, SEEDS>(n_code, uzd, n_uxu, n_uxd, n_uyu, n_uyd, uc, n_uzd, n_lxd,
                                     n_lyd, n_lzd, (unsigned)kn < (unsigned)nk, gcol + SKD * kn,
                                     gcell);
     uc = uzd;
