@@ -200,19 +200,20 @@ static int fit_shape(const void* fn, size_t warp_bytes, int regs, int max_thread
       ++G;
     if (group_hdr_bytes(G, meta_smem, max_nb) + (size_t)G * gw * warp_bytes <= budget) {
       if (groups_req > 0) G = std::min(G, groups_req);
-      for (;;) {  // shrink until one CTA fits
+      for (; G >= 1; --G) {  // shrink until one CTA fits
         smem = group_hdr_bytes(G, meta_smem, max_nb) + (size_t)G * gw * warp_bytes;
         ADT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int occ = 0;
         ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, G * gw * 32, smem));
-        if (occ >= 1) break;
-        if (G == 1) return set_error(ADT_EINVAL, "batch: no launch shape fits on this device");
-        --G;
+        if (occ >= 1) {
+          groups = G;
+          return ADT_OK;
+        }
       }
-      groups = G;
-      return ADT_OK;
     }
-    if (gw == 1) return set_error(ADT_EINVAL, "batch: brick tile does not fit in shared memory");
+    // no group count fits at this width (shared memory, or the occupancy
+    // calculator's register and carve-out limits): try a narrower group
+    if (gw == 1) return set_error(ADT_EINVAL, "batch: no launch shape fits on this device");
     --gw;
   }
 }
