@@ -76,6 +76,7 @@ SIGNATURES = {
     "adt_eikonal_three_d_device_noalloc": (C.c_int, [_P, _P, _D, _I64, _I64, _I64, _D, C.c_int,
                                                      _P, _P, _P]),
     "adt_abi_struct_sizes": (C.c_int, [_P, _I32]),
+    "adt_tile_layout": (C.c_int, [_I32, _P]),
     "adt_batch_opts_default": (None, [_P]),
     "adt_batch_create": (C.c_int, [_P, _I32, _P, _P, _P, _P, _I32, _P, _P, _P]),
     "adt_batch_destroy": (C.c_int, [_P]),

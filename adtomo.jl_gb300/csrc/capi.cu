@@ -97,6 +97,18 @@ const char* adt_last_error(void) { return g_err; }
 
 const char* adt_version(void) { return "adtomo-gb300 0.1 (sm_103a)"; }
 
+int adt_tile_layout(int32_t bk, int32_t* out) {
+  if (!out || (bk != 16 && bk != 32 && bk != 64))
+    return set_error(ADT_EINVAL, "tile_layout: bk must be 16, 32 or 64");
+  out[0] = adt::tile_row_stride(bk);
+  out[1] = adt::itile_row_stride(bk);
+  out[2] = adt::tile_col_stride(bk, true);
+  out[3] = adt::tile_col_stride(bk, false);
+  out[4] = adt::tile_elems(bk);
+  out[5] = adt::itile_elems(bk);
+  return ADT_OK;
+}
+
 int adt_abi_struct_sizes(int64_t* out, int n) {
   const int64_t sz[3] = {(int64_t)sizeof(adt_solve_status), (int64_t)sizeof(adt_batch_opts),
                          (int64_t)sizeof(adt_batch_stats)};

@@ -60,6 +60,13 @@ int adt_device_count(void);
  * sizeof(adt_batch_opts), out[2] = sizeof(adt_batch_stats).  Writes at most
  * n entries and returns the number of structs (3); never fails. */
 int adt_abi_struct_sizes(int64_t* out, int n);
+/* Shared-memory tile layout of the 3D brick sweeps (bricks of 8 x 4 columns,
+ * bk = 16, 32 or 64 cells deep), in elements: out[0] = row stride of a halo
+ * tile, out[1] = row stride of an interior tile, out[2] = column stride when
+ * the j and k sweep directions agree, out[3] = when they differ, out[4] =
+ * elements of a halo tile, out[5] = of an interior tile.  For checks of the
+ * index arithmetic; ADT_EINVAL for another bk. */
+int adt_tile_layout(int32_t bk, int32_t* out);
 
 /* ------------------------------------------------------------------------
  * 2D op: replaces Eikonal (Eikonal.cpp:20-46, Compute :74-127).
