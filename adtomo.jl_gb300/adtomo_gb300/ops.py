@@ -117,6 +117,10 @@ class Batch3D:
     Each evaluation (run) takes the slowness of every field, t_obs and weight
     (concatenated per solve over the stations of its field; t_obs == -1 is a
     missing pick) and returns (misfit, t_pred, [grad per field], status).
+    Options are the fields of adt_batch_opts (include/adtomo_gpu.h); in
+    particular wake_tol / adj_wake_tol (FP32 only, default 0 = exact brick
+    skipping) let bricks that moved by at most that much (seconds; relative
+    for the adjoint) leave their neighbours asleep.
     """
 
     def __init__(self, fields, stations, solve_field, src_xyz, precision=ADT_F32, tol=1e-6,
