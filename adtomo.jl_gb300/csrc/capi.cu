@@ -298,7 +298,9 @@ int adt_batch_create(adt_batch** out, int32_t n_fields, const int32_t* dims, con
                      const adt_batch_opts* opts) {
   if (!out) return set_error(ADT_EINVAL, "batch: null output handle");
   *out = nullptr;
-  int rc = check_device();
+  int rc = batch_check_args(n_fields, dims, h, nsta, n_solves, solve_field, src_xyz, opts);
+  if (rc) return rc;
+  rc = check_device();
   if (rc) return rc;
   BatchPlan* p = nullptr;
   rc = batch_create(&p, n_fields, dims, h, nsta, sta_xyz, n_solves, solve_field, src_xyz, opts);

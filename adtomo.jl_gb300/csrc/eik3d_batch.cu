@@ -249,10 +249,9 @@ static int apply_shapes(BatchPlan* P, int fwd_gw, int fwd_groups, int adj_gw, in
   return ADT_OK;
 }
 
-int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* hh,
-                 const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
-                 const int32_t* solve_field, const double* src_xyz, const adt_batch_opts* opts) {
-  *out = nullptr;
+int batch_check_args(int32_t n_fields, const int32_t* dims, const double* hh, const int32_t* nsta,
+                     int32_t n_solves, const int32_t* solve_field, const double* src_xyz,
+                     const adt_batch_opts* opts) {
   adt_batch_opts o;
   batch_opts_default(&o);
   if (opts) o = *opts;
@@ -269,6 +268,18 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     return set_error(ADT_EINVAL, "batch: wake_tol and adj_wake_tol must be finite and >= 0");
   if (o.bk != 0 && o.bk != 16 && o.bk != 32 && o.bk != 64)
     return set_error(ADT_EINVAL, "batch: bk must be 0, 16, 32 or 64");
+  return ADT_OK;
+}
+
+int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* hh,
+                 const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
+                 const int32_t* solve_field, const double* src_xyz, const adt_batch_opts* opts) {
+  *out = nullptr;
+  int rc0 = batch_check_args(n_fields, dims, hh, nsta, n_solves, solve_field, src_xyz, opts);
+  if (rc0) return rc0;
+  adt_batch_opts o;
+  batch_opts_default(&o);
+  if (opts) o = *opts;
   auto P = std::make_unique<BatchPlan>();
   P->opts = o;
   if (o.ref_compat) P->opts.max_iter = std::min(o.max_iter, 20);

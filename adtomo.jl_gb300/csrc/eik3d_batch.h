@@ -7,6 +7,10 @@ namespace adt {
 struct BatchPlan;
 
 void batch_opts_default(adt_batch_opts* o);
+// Host-only checks of the plan's arguments and options (no device work).
+int batch_check_args(int32_t n_fields, const int32_t* dims, const double* h, const int32_t* nsta,
+                     int32_t n_solves, const int32_t* solve_field, const double* src_xyz,
+                     const adt_batch_opts* opts);
 int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const double* h,
                  const int32_t* nsta, const double* sta_xyz, int32_t n_solves,
                  const int32_t* solve_field, const double* src_xyz, const adt_batch_opts* opts);

@@ -79,6 +79,15 @@ def test_size_mismatch_is_rejected_host_side():
         A.eikonal3d(np.zeros(10), np.ones(10), 1.0, 3, 3, 3, 1e-6)
 
 
+@pytest.mark.parametrize("kw", [{"wake_tol": -1.0}, {"adj_wake_tol": float("nan")}, {"bk": 8},
+                                {"precision": 7}, {"max_iter": 0}, {"tol": -1.0},
+                                {"ref_compat": True}])
+def test_batch_options_rejected_host_side(kw):
+    with pytest.raises(A.AdtError) as e:
+        A.Batch3D([(8, 8, 8, 1.0)], [np.zeros((1, 3))], [0], [[1.0, 1.0, 1.0]], **kw)
+    assert e.value.name == "ADT_EINVAL"
+
+
 @pytest.mark.skipif(A.lib().adt_device_count() > 0, reason="a GPU is present")
 def test_valid_call_without_gpu_reports_nodev():
     with pytest.raises(A.AdtError) as e:
