@@ -88,6 +88,24 @@ def test_batch_options_rejected_host_side(kw):
     assert e.value.name == "ADT_EINVAL"
 
 
+def test_batch_null_handle_is_rejected():
+    import ctypes as C
+    L = A.lib()
+    one = np.zeros(4)
+    assert L.adt_batch_upload(None, None, None, None) == -1
+    assert L.adt_batch_run_resident(None) == -1
+    assert L.adt_batch_autotune(None, 1) == -1
+    assert L.adt_batch_set_source_slowness(None, None) == -1
+    assert L.adt_batch_download(None, None, None, None, None) == -1
+    assert L.adt_batch_run(None, one.ctypes.data_as(C.c_void_p), None, None, None, None, None,
+                           None) == -1
+    assert L.adt_batch_stats_get(None, None) == -1
+    assert L.adt_batch_stream(None) is None
+    assert L.adt_batch_device_buffer(None, 0) is None
+    assert L.adt_batch_destroy(None) == 0
+    assert b"null handle" in L.adt_last_error() or b"null" in L.adt_last_error()
+
+
 @pytest.mark.skipif(A.lib().adt_device_count() > 0, reason="a GPU is present")
 def test_valid_call_without_gpu_reports_nodev():
     with pytest.raises(A.AdtError) as e:
