@@ -31,6 +31,8 @@ __host__ __device__ __forceinline__ T rmax(T a, T b) {
 // column, BK cells deep along k (the contiguous axis).
 constexpr int BI = 8;
 constexpr int BJ = 4;
+// Brick depth of the plain single-solve 3D path (the batched plan chooses its own).
+constexpr int SBK = 32;
 
 // Shared-memory tile of one brick with a one-cell halo on every side:
 // column (pi, pj) for pi in [-1, BI], pj in [-1, BJ]; slot k+1 for k in

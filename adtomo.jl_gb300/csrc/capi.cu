@@ -81,6 +81,11 @@ int check3d(int64_t m, int64_t n, int64_t l, double h, double tol) {
                      (long long)n, (long long)l);
   if (m > BI * 2047 || n > BJ * 2047 || l > (1 << 20) || m * n * l > ((int64_t)1 << 34))
     return set_error(ADT_EINVAL, "eikonal3d: grid too large");
+  // brick coordinates are packed in 11/11/10 bits (pack_brick): at most 1023
+  // bricks along k
+  if (make_geom((int)m, (int)n, (int)l, SBK).nbz > 1023)
+    return set_error(ADT_EINVAL, "eikonal3d: l = %lld is too deep (at most %d)", (long long)l,
+                     SBK * 1023);
   if (!(h > 0.0) || !std::isfinite(h)) return set_error(ADT_EINVAL, "eikonal3d: h must be finite and > 0");
   if (!(tol >= 0.0)) return set_error(ADT_EINVAL, "eikonal3d: tol must be >= 0");
   return ADT_OK;

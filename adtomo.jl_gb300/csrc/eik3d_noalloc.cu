@@ -25,6 +25,7 @@
 //  - Nothing is left for the next call to rely on: the previous iterate is
 //    overwritten each iteration, the level list on each call, and the error
 //    word is cleared before each use.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -80,38 +81,12 @@ NoAllocDevice& na_device(int dev) {
   return d[dev];
 }
 
-}  // namespace
-
-}  // namespace adt
-
-using namespace adt;
-
-extern "C" int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double h,
-                                                  int64_t m, int64_t n, int64_t l, double tol,
-                                                  int verbose, double* u,
-                                                  adt_solve_status* status, void* stream) {
-  if (m < 2 || n < 2 || l < 2)
-    return set_error(ADT_EINVAL, "eikonal3d_noalloc: need m, n, l >= 2 (got %lld x %lld x %lld)",
-                     (long long)m, (long long)n, (long long)l);
-  if (m > BI * 2047 || n > BJ * 2047 || m * n * l > (int64_t)ADT_NOALLOC_MAX_CELLS)
-    return set_error(ADT_EINVAL,
-                     "eikonal3d_noalloc: %lld cells exceed the fixed scratch limit of %d cells "
-                     "(use adt_eikonal_three_d_device for larger grids)",
-                     (long long)(m * n * l), ADT_NOALLOC_MAX_CELLS);
-  if (!(h > 0.0) || !(tol >= 0.0)) return set_error(ADT_EINVAL, "eikonal3d_noalloc: bad h or tol");
-  if (!u0 || !f || !u) return set_error(ADT_EINVAL, "eikonal3d_noalloc: null array");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-    cudaGetLastError();
-    return set_error(ADT_ENODEV, "no CUDA device available");
-  }
-  int dev = 0;
-  ADT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= NA_MAX_DEVICES)
-    return set_error(ADT_EINVAL, "eikonal3d_noalloc: device %d beyond the supported %d", dev,
-                     NA_MAX_DEVICES);
-  NoAllocDevice& D = na_device(dev);
-  std::lock_guard<std::mutex> lock(D.mu);
+// The solve itself, on the locked device D.  Sets `enqueued` once work has
+// been queued on `st`, so that the caller can drain the stream when an
+// error cuts the call short.
+int na_solve(NoAllocDevice& D, const double* u0, const double* f, double h, const Geom& g,
+             double tol, int verbose, double* u, adt_solve_status* status, cudaStream_t st,
+             bool& enqueued) {
   if (!D.base) {  // once per device, with that device current
     void* p = nullptr;
     ADT_CUDA(cudaGetSymbolAddress(&p, adt_noalloc_scratch));
@@ -122,14 +97,13 @@ extern "C" int adt_eikonal_three_d_device_noalloc(const double* u0, const double
                                   (int)(FWD_WPB * FWD_WARP_SMEM)));
     D.attr_set = true;
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  const Geom g = make_geom((int)m, (int)n, (int)l, SBK);
   if (!na_levels(g, D)) return set_error(ADT_EINVAL, "eikonal3d_noalloc: grid has too many bricks");
   const int nbricks = D.start[g.nlev];
   double* uold = reinterpret_cast<double*>(D.base);
   uint32_t* bricks = reinterpret_cast<uint32_t*>(D.base + NA_UOLD_BYTES);
   unsigned long long* err_word = reinterpret_cast<unsigned long long*>(D.base + NA_ERR_OFF);
   const size_t bytes = (size_t)g.ncell * sizeof(double);
+  enqueued = true;
   ADT_CUDA(cudaMemcpyAsync(bricks, D.bricks, nbricks * sizeof(uint32_t), cudaMemcpyHostToDevice,
                            st));
   ADT_CUDA(cudaMemcpyAsync(u, u0, bytes, cudaMemcpyDeviceToDevice, st));
@@ -165,4 +139,58 @@ extern "C" int adt_eikonal_three_d_device_noalloc(const double* u0, const double
     status->adj_converged = 0;
   }
   return ADT_OK;
+}
+
+}  // namespace
+}  // namespace adt
+
+using namespace adt;
+
+extern "C" int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double h,
+                                                  int64_t m, int64_t n, int64_t l, double tol,
+                                                  int verbose, double* u,
+                                                  adt_solve_status* status, void* stream) {
+  if (m < 2 || n < 2 || l < 2)
+    return set_error(ADT_EINVAL, "eikonal3d_noalloc: need m, n, l >= 2 (got %lld x %lld x %lld)",
+                     (long long)m, (long long)n, (long long)l);
+  // each extent is bounded before the product is formed, so the product
+  // cannot overflow
+  if (m > BI * 2047 || n > BJ * 2047 || l > (int64_t)ADT_NOALLOC_MAX_CELLS ||
+      m * n * l > (int64_t)ADT_NOALLOC_MAX_CELLS)
+    return set_error(ADT_EINVAL,
+                     "eikonal3d_noalloc: %lld x %lld x %lld cells exceed the fixed scratch limit "
+                     "of %d cells (use adt_eikonal_three_d_device for larger grids)",
+                     (long long)m, (long long)n, (long long)l, ADT_NOALLOC_MAX_CELLS);
+  // brick coordinates are packed in 11/11/10 bits (pack_brick)
+  if (make_geom((int)m, (int)n, (int)l, SBK).nbz > 1023)
+    return set_error(ADT_EINVAL, "eikonal3d_noalloc: l = %lld is too deep (at most %d)",
+                     (long long)l, SBK * 1023);
+  if (!(h > 0.0) || !std::isfinite(h))
+    return set_error(ADT_EINVAL, "eikonal3d_noalloc: h must be finite and > 0");
+  if (!(tol >= 0.0)) return set_error(ADT_EINVAL, "eikonal3d_noalloc: tol must be >= 0");
+  if (!u0 || !f || !u) return set_error(ADT_EINVAL, "eikonal3d_noalloc: null array");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_error(ADT_ENODEV, "no CUDA device available");
+  }
+  int dev = 0;
+  ADT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NA_MAX_DEVICES)
+    return set_error(ADT_EINVAL, "eikonal3d_noalloc: device %d beyond the supported %d", dev,
+                     NA_MAX_DEVICES);
+  NoAllocDevice& D = na_device(dev);
+  std::lock_guard<std::mutex> lock(D.mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  bool enqueued = false;
+  const int rc = na_solve(D, u0, f, h, make_geom((int)m, (int)n, (int)l, SBK), tol, verbose, u,
+                          status, st, enqueued);
+  // On an error after work was queued, wait for that work before the lock is
+  // released: a later call must not reuse the scratch under it.  The error
+  // of the wait itself is not reported over the first one.
+  if (rc != ADT_OK && enqueued) {
+    cudaStreamSynchronize(st);
+    cudaGetLastError();
+  }
+  return rc;
 }

@@ -5,7 +5,6 @@
 
 namespace adt {
 
-constexpr int SBK = 32;        // brick depth of the single-solve path
 constexpr int FWD_WPB = 4;     // warps (bricks) per CTA, forward
 constexpr int ADJ_WPB = 2;     // warps per CTA, adjoint
 constexpr size_t FWD_WARP_SMEM = (tile_elems(SBK) + itile_elems(SBK)) * sizeof(double);

@@ -6,8 +6,8 @@
  * EikonalThreeD / EikonalThreeDGrad (deps/CustomOps/Eikonal3D/EikonalThreeD.cpp),
  * which the Julia functions eikonal(...) and eikonal3d(...) of
  * src/eikonal_op.jl load through ADCME.load_op_and_grad.  A Julia caller binds
- * these symbols with ccall; the Python package
- * adtomo_gb300 binds them with ctypes.
+ * these symbols with ccall; the Python package adtomo_gb300 binds them with
+ * ctypes.
  *
  * Conventions
  *  - Plain pointers and sizes only.  Unless a function name ends in _device,

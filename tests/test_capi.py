@@ -111,3 +111,46 @@ def test_valid_call_without_gpu_reports_nodev():
     with pytest.raises(A.AdtError) as e:
         A.eikonal3d(np.full(27, 1000.0), np.ones(27), 1.0, 3, 3, 3, 1e-6)
     assert e.value.name == "ADT_ENODEV"
+
+
+def test_eikonal3d_rejects_grids_deeper_than_the_brick_packing():
+    """Brick coordinates are packed in 11/11/10 bits: more than 1023 bricks of
+    32 cells along k would wrap, so the plain 3D entry points reject such a
+    grid before any device work."""
+    import ctypes as C
+    L = A.lib()
+    st = _lib.SolveStatus()
+    for l in (32 * 1023 + 1, 40000):
+        assert L.adt_eikonal_three_d_device(None, None, 1.0, 2, 2, l, 1e-6, 0, None,
+                                            C.byref(st), None) == -1
+        assert b"too deep" in L.adt_last_error()
+    # the deepest accepted grid passes the size checks (and fails on the null arrays)
+    assert L.adt_eikonal_three_d_device(None, None, 1.0, 2, 2, 32 * 1023, 1e-6, 0, None,
+                                        C.byref(st), None) == -1
+    assert b"null array" in L.adt_last_error()
+
+
+@pytest.mark.parametrize("dims,msg", [((2, 2, 40000), b"too deep"),
+                                      ((16376, 8188, 1 << 40), b"scratch limit"),
+                                      ((8, 8, (1 << 62) // 64 + 1), b"scratch limit"),
+                                      ((64, 64, 65), b"scratch limit")])
+def test_noalloc_rejects_sizes_host_side(dims, msg):
+    """The no-allocation entry point bounds every extent before forming the
+    cell count (a huge l must not wrap the product below the limit) and
+    rejects grids deeper than the brick packing, before any device work."""
+    import ctypes as C
+    L = A.lib()
+    st = _lib.SolveStatus()
+    m, n, l = dims
+    assert L.adt_eikonal_three_d_device_noalloc(None, None, 1.0, m, n, l, 1e-6, 0, None,
+                                                C.byref(st), None) == -1
+    assert msg in L.adt_last_error()
+
+
+def test_noalloc_rejects_infinite_spacing_like_the_plain_entry_point():
+    import ctypes as C
+    L = A.lib()
+    st = _lib.SolveStatus()
+    for fn in (L.adt_eikonal_three_d_device_noalloc, L.adt_eikonal_three_d_device):
+        assert fn(None, None, float("inf"), 4, 4, 4, 1e-6, 0, None, C.byref(st), None) == -1
+        assert b"finite" in L.adt_last_error()

@@ -5,9 +5,10 @@ device heap, a host with a memory budget fixed at start-up).  This entry
 point runs the plain FP64 3D forward on caller-provided device buffers and
 takes its scratch from a fixed array inside the library.  Its results must
 equal the existing entry point adt_eikonal_three_d_device, which uses the
-same kernels: FP64 travel times bit-identical (the tolerance of the plain
-FP64 parity tests), on two calls in a row, so the shared scratch carries
-nothing over from one call to the next.
+same kernels, and the oracle's restatement of the reference's forward
+(Eikonal3D.cpp:71-94, same tolerance and 20-iteration cap): FP64 travel times
+bit-identical (the tolerance of the plain FP64 parity tests), on two calls in
+a row, so the shared scratch carries nothing over from one call to the next.
 
 This file is collected last so that, when it fails, a run stopping at the
 first failure has already run every other test.
@@ -68,10 +69,13 @@ def test_noalloc_matches_existing_entry_point(torch_cuda, name, dims, h, tol):
     src = (rng.uniform(0, m - 1), rng.uniform(0, n - 1), rng.uniform(0, l - 1))
     u0 = O.src_u0(f, h, src)
     ref, ref_st = _run(L.adt_eikonal_three_d_device, torch, u0, f, h, tol)
+    orc, orc_it, orc_err = O.eik3d_forward(u0, f, h, tol)
     for _ in range(2):  # two calls in a row share the same scratch
         got, st = _run(L.adt_eikonal_three_d_device_noalloc, torch, u0, f, h, tol)
         assert np.array_equal(got, ref)
         assert st == ref_st
+        assert np.array_equal(got, orc)
+        assert st[0] == orc_it and st[2] == orc_err
 
 
 def test_noalloc_rejects_grids_above_the_scratch_limit(torch_cuda):
