@@ -82,7 +82,7 @@ SIGNATURES = {
     "adt_batch_destroy": (C.c_int, [_P]),
     "adt_batch_run": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "adt_batch_upload": (C.c_int, [_P, _P, _P, _P]),
-    "adt_batch_set_source_slowness": (C.c_int, [_P, _P]),
+    "adt_batch_set_source_velocity": (C.c_int, [_P, _P]),
     "adt_batch_autotune": (C.c_int, [_P, _I32]),
     "adt_batch_run_resident": (C.c_int, [_P]),
     "adt_batch_download": (C.c_int, [_P, _P, _P, _P, _P]),

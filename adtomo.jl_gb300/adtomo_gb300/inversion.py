@@ -178,8 +178,7 @@ class TravelTimeInversion:
         self.lambda_p, self.sh, self.sv = float(lambda_p), int(smooth_hor), int(smooth_ver)
         self.plan = Batch3D([(m, n, l, h)], [self.events], np.zeros(S, np.int32), self.stations,
                             precision=precision, tol=tol, max_iter=max_iter, **plan_kw)
-        check(lib().adt_batch_set_source_slowness(self.plan._h, _ptr(np.ascontiguousarray(
-            1.0 / self.vel0))))
+        self.plan.set_source_velocity([self.vel0])
         self.evaluations = 0
         self.last_status = None
 

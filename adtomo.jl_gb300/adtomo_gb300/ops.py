@@ -114,6 +114,10 @@ class Batch3D:
     fields:   list of (m, n, l, h)
     stations: list of (S_f, 3) arrays of fractional 0-based node coordinates
     solve_field, src_xyz: per solve, the field index and the source position
+    The near-source initial values follow scripts/gene_obs.jl:42-51 (the
+    evaluation's slowness at the source's (ceil x, ceil y) column, one value
+    per depth plane); set_source_velocity switches to scripts/inversion.jl's
+    rule (a fixed vel0 per node).
     Each evaluation (run) takes the slowness of every field, t_obs and weight
     (concatenated per solve over the stations of its field; t_obs == -1 is a
     missing pick) and returns (misfit, t_pred, [grad per field], status).
@@ -215,6 +219,20 @@ class Batch3D:
 
     def run_resident(self):
         check(self._L.adt_batch_run_resident(self._h))
+
+    def set_source_velocity(self, vel0):
+        """Near-source initial values from the fixed velocity models vel0 (one
+        per field): r * h / vel0[node] at the 8 nodes around each source, the
+        rule of scripts/inversion.jl:52-60 (adt_batch_set_source_velocity).
+        None returns to the default rule of scripts/gene_obs.jl:42-51, which
+        uses the evaluation's own slowness."""
+        if vel0 is None:
+            check(self._L.adt_batch_set_source_velocity(self._h, None))
+            return
+        v = np.concatenate([_f64(a, "vel0").ravel() for a in vel0])
+        if v.size != sum(self.ncell):
+            raise AdtError(-1, "vel0 size does not match the fields")
+        check(self._L.adt_batch_set_source_velocity(self._h, _ptr(v)))
 
     def download(self):
         mis = C.c_double(0)

@@ -327,9 +327,9 @@ int adt_batch_upload(adt_batch* b, const double* slowness, const double* t_obs,
   return batch_upload(b->plan, slowness, t_obs, weight);
 }
 
-int adt_batch_set_source_slowness(adt_batch* b, const double* slowness0) {
+int adt_batch_set_source_velocity(adt_batch* b, const double* vel0) {
   if (!b) return set_error(ADT_EINVAL, "batch: null handle");
-  return batch_set_source_slowness(b->plan, slowness0);
+  return batch_set_source_velocity(b->plan, vel0);
 }
 
 int adt_batch_autotune(adt_batch* b, int32_t reps) {

@@ -26,10 +26,15 @@ __global__ void k_to_t_f32(const double* __restrict__ a, float* __restrict__ b, 
     b[i] = (float)a[i];
 }
 
-// FP64 near-source initial values: sqrt(dx^2+dy^2+dz^2) * f * h at the 8
-// nodes around each source (scripts/gene_obs.jl:44-51, order ceil/floor).
+// FP64 near-source initial values at the 8 nodes (i, j, k) around each
+// source, from the distance r = sqrt(dx^2+dy^2+dz^2) (dx = x - i, ...):
+//  - default (vel == 0): r * f * h with one slowness per depth plane, taken
+//    from the evaluation's slowness at the (ceil x, ceil y) column
+//    (scripts/gene_obs.jl:42-51: slowness_pu / slowness_pd);
+//  - vel != 0: r * h / vel0[i, j, k], vel0 a fixed velocity model
+//    (scripts/inversion.jl:52-60).
 template <class T>
-__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields, int fixed,
+__global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields, int vel,
                            unsigned long long* cost) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
@@ -41,11 +46,17 @@ __global__ void k_src_init(SolveDev* solves, int n, const FieldDev<T>* fields, i
     for (int b = 0; b < 2; ++b)
       for (int c = 0; c < 2; ++c) {
         const double dx = sd.sx - xs[a], dy = sd.sy - ys[b], dz = sd.sz - zs[c];
-        const int64_t p = ((int64_t)xs[a] * fd.g.n + ys[b]) * fd.g.l + zs[c];
         const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                               __dmul_rn(dz, dz)));
-        const double f = fixed ? fd.f0[p] : fd.f64[p];
-        sd.v0[a * 4 + b * 2 + c] = __dmul_rn(__dmul_rn(r, f), fd.h);
+        double v;
+        if (vel) {
+          const int64_t p = ((int64_t)xs[a] * fd.g.n + ys[b]) * fd.g.l + zs[c];
+          v = __ddiv_rn(__dmul_rn(r, fd.h), fd.vel0[p]);
+        } else {
+          const int64_t q = ((int64_t)sd.xc * fd.g.n + sd.yc) * fd.g.l + zs[c];
+          v = __dmul_rn(__dmul_rn(r, fd.f64[q]), fd.h);
+        }
+        sd.v0[a * 4 + b * 2 + c] = v;
       }
 }
 
@@ -135,7 +146,7 @@ struct BatchPlan {
   };
   std::vector<Chunk> chunks;
   // device
-  DevBuf d_slow64, d_slow0, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
+  DevBuf d_slow64, d_vel0, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
   DevBuf d_levels, d_lstart, d_fields, d_solves, d_order, d_uoff;
   DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
   DevBuf d_gdense;  // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
@@ -145,7 +156,7 @@ struct BatchPlan {
   int64_t snap_stride = 0;
   std::vector<adt_solve_status> h_status;
   int uploaded = 0;  // bits: 1 slowness, 2 t_obs, 4 weight
-  bool src_fixed = false;  // near-source values from d_slow0 (batch_set_source_slowness)
+  bool src_vel = false;  // near-source values from d_vel0 (batch_set_source_velocity)
   // launch shapes
   KernelSet ks;
   int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
@@ -397,7 +408,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
 #define R_(b, n) \
   if ((rc = R(b, n))) return rc;
   R_(P->d_slow64, P->ncell_total * 8);
-  R_(P->d_slow0, P->ncell_total * 8);
+  R_(P->d_vel0, P->ncell_total * 8);
   R_(P->d_slowT, P->f64 ? 16 : P->ncell_t_total * 4);
   R_(P->d_sta, (size_t)sofs * 3 * 8);
   R_(P->d_tobs, P->nobs * 8);
@@ -446,7 +457,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].g = P->geoms[f];
       fdv[f].h = P->h[f];
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
-      fdv[f].f0 = P->d_slow0.as<double>() + P->cell_off[f];
+      fdv[f].vel0 = P->d_vel0.as<double>() + P->cell_off[f];
       fdv[f].f = fdv[f].f64;
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
@@ -462,7 +473,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].g = P->geoms[f];
       fdv[f].h = P->h[f];
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
-      fdv[f].f0 = P->d_slow0.as<double>() + P->cell_off[f];
+      fdv[f].vel0 = P->d_vel0.as<double>() + P->cell_off[f];
       fdv[f].f = P->d_slowT.as<float>() + P->cell_off_t[f];  // 64-byte aligned (16-byte loads)
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
@@ -589,7 +600,7 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
                                                            P.geoms[f].ncell);
   k_src_init<T><<<(P.ns + 127) / 128, 128, 0, st>>>(P.d_solves.as<SolveDev>(), P.ns,
                                                      P.d_fields.as<FieldDev<T>>(),
-                                                     P.src_fixed ? 1 : 0,
+                                                     P.src_vel ? 1 : 0,
                                                      P.d_cost.as<unsigned long long>());
   ADT_CUDA(cudaMemsetAsync(P.d_grad.p, 0, P.ncell_total * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
@@ -723,21 +734,21 @@ int batch_autotune(BatchPlan* P, int reps) {
   return apply_shapes(P, best_f, 0, best_a, 0);
 }
 
-int batch_set_source_slowness(BatchPlan* P, const double* slowness0) {
-  if (slowness0) {
+int batch_set_source_velocity(BatchPlan* P, const double* vel0) {
+  if (vel0) {
     for (int64_t i = 0; i < P->ncell_total; ++i)
-      if (!(slowness0[i] > 0.0) || !std::isfinite(slowness0[i]))
-        return set_error(ADT_EINVAL, "batch: source slowness must be finite and > 0 (cell %lld)",
+      if (!(vel0[i] > 0.0) || !std::isfinite(vel0[i]))
+        return set_error(ADT_EINVAL, "batch: source velocity must be finite and > 0 (cell %lld)",
                          (long long)i);
-    ADT_CUDA(cudaMemcpyAsync(P->d_slow0.p, slowness0, P->ncell_total * 8, cudaMemcpyHostToDevice,
+    ADT_CUDA(cudaMemcpyAsync(P->d_vel0.p, vel0, P->ncell_total * 8, cudaMemcpyHostToDevice,
                              P->stream));
   }
   ADT_CUDA(cudaStreamSynchronize(P->stream));
-  if (P->src_fixed != (slowness0 != nullptr) && P->graph) {  // the source kernel's argument changes
+  if (P->src_vel != (vel0 != nullptr) && P->graph) {  // the source kernel's argument changes
     cudaGraphExecDestroy(P->graph);
     P->graph = nullptr;
   }
-  P->src_fixed = slowness0 != nullptr;
+  P->src_vel = vel0 != nullptr;
   return ADT_OK;
 }
 

@@ -17,7 +17,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
 void batch_destroy(BatchPlan* p);
 int batch_upload(BatchPlan* p, const double* slowness, const double* t_obs, const double* weight);
 int batch_run_resident(BatchPlan* p);
-int batch_set_source_slowness(BatchPlan* p, const double* slowness0);
+int batch_set_source_velocity(BatchPlan* p, const double* vel0);
 int batch_autotune(BatchPlan* p, int reps);
 int batch_download(BatchPlan* p, double* misfit, double* t_pred, double* grad,
                    adt_solve_status* status);

@@ -34,7 +34,7 @@ struct FieldDev {
   double h;
   const T* f;               // slowness, compute precision
   const double* f64;        // slowness, FP64 (gradient)
-  const double* f0;         // slowness for the near-source initial values, FP64
+  const double* vel0;       // fixed velocity model for the near-source values, FP64
   const uint32_t* bricks;   // level-ordered bricks
   const int* lstart;        // nlev + 1
   const double* sta;        // receivers, 3 per station
@@ -107,8 +107,9 @@ __host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_
   return b;
 }
 
-// Initial value of the implicit u0 (scripts/gene_obs.jl:44-51): 1000, or the
-// FP64 distance value at the 8 nodes around the source.
+// Initial value of the implicit u0: 1000, or the FP64 near-source value at
+// the 8 nodes around the source (k_src_init; scripts/gene_obs.jl:42-51,
+// scripts/inversion.jl:52-60).
 __device__ __forceinline__ double u0_at(const SolveDev& s, int i, int j, int k) {
   const bool xi = (i == s.xc) || (i == s.xf);
   const bool yj = (j == s.yc) || (j == s.yf);

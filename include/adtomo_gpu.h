@@ -150,9 +150,12 @@ int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double
  *       coordinates, concatenated over fields)
  *   solves s = 0..n_solves-1: field solve_field[s], source src_xyz[3s..3s+2]
  *       (fractional 0-based node coordinates).  u0 is 1000 everywhere except
- *       the 8 nodes around the source, which get dist * f * h computed in FP64
- *       (scripts/gene_obs.jl:44-51); no gradient flows through u0, as in
- *       scripts/inversion.jl where u0 is built from vel0.
+ *       the 8 nodes (i, j, k) around the source (ceil and floor of each
+ *       coordinate), which get r * f * h in FP64, r their distance to the
+ *       source, f the slowness at (ceil x, ceil y, k): one slowness per depth
+ *       plane, as scripts/gene_obs.jl:42-51 builds it
+ *       (adt_batch_set_source_velocity switches to scripts/inversion.jl's
+ *       rule).  No gradient flows through u0.
  *   picks: t_obs and weight, nsta[solve_field[s]] per solve, concatenated;
  *       t_obs == -1 marks a missing pick (scripts/inversion.jl:81).
  *   outputs: misfit = sum weight*(t_obs - t_pred)^2, t_pred (like t_obs),
@@ -204,14 +207,15 @@ int adt_batch_destroy(adt_batch* b);
 int adt_batch_run(adt_batch* b, const double* slowness, const double* t_obs, const double* weight,
                   double* misfit, double* t_pred, double* grad, adt_solve_status* status);
 
-/* Slowness used for the near-source initial values (the 8 nodes around each
- * source get distance * h * slowness).  By default that is the slowness of
- * the evaluation itself.  scripts/inversion.jl:52-60 instead builds u0 from
- * the starting model vel0 and keeps it while the model changes: pass that
- * model's slowness here (all fields, as in adt_batch_run) to do the same.
- * NULL returns to the default.  The near-source values are constants of the
- * evaluation either way: the gradient does not flow through them. */
-int adt_batch_set_source_slowness(adt_batch* b, const double* slowness0);
+/* Near-source initial values from a fixed velocity model: the 8 nodes around
+ * each source get r * h / vel0[node] (r their distance to the source), as
+ * scripts/inversion.jl:52-60 builds u0 from the starting model vel0 and keeps
+ * it while the model changes.  vel0: all fields, concatenated like the
+ * slowness of adt_batch_run, finite and > 0.  NULL returns to the default
+ * rule of scripts/gene_obs.jl (the evaluation's own slowness; see
+ * adt_batch_create).  Either way the values are constants of the
+ * evaluation: no gradient flows through them. */
+int adt_batch_set_source_velocity(adt_batch* b, const double* vel0);
 
 /* Autotuner of the launch shapes: after adt_batch_upload of all three
  * inputs, times the forward and the adjoint sweep kernels over candidate

@@ -432,21 +432,35 @@ int64_t orc_assemble(int dim, const double* u, const double* u0, int m, int n,
 /* Sources, receivers, misfit                                                */
 /* ------------------------------------------------------------------------ */
 
-void orc_src_u0(const double* f, int m, int n, int l, double h, double sx,
-                double sy, double sz, double* u0) {
+void orc_src_u0(const double* a, int m, int n, int l, double h, double sx,
+                double sy, double sz, int mode, double* u0) {
   const int64_t N = (int64_t)m * n * l;
   for (int64_t p = 0; p < N; ++p) u0[p] = 1000.0;
   const int xs[2] = {(int)ceil(sx), (int)floor(sx)};
   const int ys[2] = {(int)ceil(sy), (int)floor(sy)};
   const int zs[2] = {(int)ceil(sz), (int)floor(sz)};
-  /* same assignment order as gene_obs.jl:44-51 (u,u,u), (u,u,d), (u,d,u) ... */
-  for (int a = 0; a < 2; ++a)
+  /* assignment order of gene_obs.jl:44-51 and inversion.jl:53-60: (u,u,u),
+   * (u,u,d), (u,d,u), ... (when a coordinate is integral, both assignments
+   * to a node carry the same value) */
+  for (int a_ = 0; a_ < 2; ++a_)
     for (int b = 0; b < 2; ++b)
       for (int c = 0; c < 2; ++c) {
-        const int i = xs[a], j = ys[b], k = zs[c];
+        const int i = xs[a_], j = ys[b], k = zs[c];
         const int64_t p = ((int64_t)i * n + j) * l + k;
         const double dx = sx - i, dy = sy - j, dz = sz - k;
-        u0[p] = sqrt(dx * dx + dy * dy + dz * dz) * f[p] * h;
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        if (mode == ORC_SRC_INVERSION) {
+          /* sqrt(...)*h/vel0[node], inversion.jl:53-60 */
+          u0[p] = r * h / a[p];
+        } else if (mode == ORC_SRC_GENE_OBS) {
+          /* slowness_pu = fvel[ixu,iyu,izu] for the izu plane, slowness_pd =
+           * fvel[ixu,iyu,izd] for the izd plane; sqrt(...)*slowness*h,
+           * gene_obs.jl:42-51 */
+          const int64_t q = ((int64_t)xs[0] * n + ys[0]) * l + k;
+          u0[p] = r * a[q] * h;
+        } else {
+          u0[p] = r * a[p] * h;
+        }
       }
 }
 
@@ -516,6 +530,8 @@ typedef struct {
   const double* weight;
   double tol;
   int max_iter;
+  int src_mode;
+  const double* src_model; /* near-source model (NULL: the slowness) */
   const int64_t* field_off; /* cell offset per field */
   const int64_t* sta_off;   /* station offset per field */
   const int64_t* obs_off;   /* pick offset per solve */
@@ -544,7 +560,9 @@ static void* batch_worker(void* arg) {
     const int64_t N = (int64_t)m * n * l;
     const double hh = J->h[fi];
     const double* f = J->slowness + J->field_off[fi];
-    orc_src_u0(f, m, n, l, hh, J->src_xyz[3 * s], J->src_xyz[3 * s + 1], J->src_xyz[3 * s + 2], u0);
+    const double* a = J->src_model ? J->src_model + J->field_off[fi] : f;
+    orc_src_u0(a, m, n, l, hh, J->src_xyz[3 * s], J->src_xyz[3 * s + 1], J->src_xyz[3 * s + 2],
+               J->src_mode, u0);
     double ferr = 0.0;
     J->iters[s] = orc_eik3d_forward(u0, f, hh, m, n, l, J->tol, J->max_iter, u, &ferr);
     memset(gu, 0, (size_t)N * sizeof(double));
@@ -583,8 +601,10 @@ int orc_batch_misfit_grad(int n_fields, const int32_t* dims, const double* h,
                           const double* sta_xyz, int n_solves,
                           const int32_t* solve_field, const double* src_xyz,
                           const double* t_obs, const double* weight, double tol,
-                          int max_iter, int nthreads, double* misfit,
+                          int max_iter, int nthreads, int src_mode,
+                          const double* src_model, double* misfit,
                           double* t_pred, double* grad, int32_t* iters) {
+  if (src_mode == ORC_SRC_INVERSION && !src_model) return -1;
   if (nthreads < 1) nthreads = 1;
   if (nthreads > n_solves && n_solves > 0) nthreads = n_solves;
   int64_t* field_off = (int64_t*)malloc(sizeof(int64_t) * (n_fields + 1));
@@ -619,6 +639,8 @@ int orc_batch_misfit_grad(int n_fields, const int32_t* dims, const double* h,
     J->weight = weight;
     J->tol = tol;
     J->max_iter = max_iter;
+    J->src_mode = src_mode;
+    J->src_model = src_model;
     J->field_off = field_off;
     J->sta_off = sta_off;
     J->obs_off = obs_off;

@@ -56,12 +56,21 @@ int64_t orc_assemble(int dim, const double* u, const double* u0, int m, int n,
                      int l, int ix, int jx, int64_t cap, int64_t* rows,
                      int64_t* cols, double* vals, double* rhs_mask);
 
-/* Near-source initial condition, scripts/gene_obs.jl:44-52 and
- * scripts/inversion.jl:52-60: u0 = 1000 everywhere, and the 8 nodes around the
- * fractional source (sx,sy,sz) (0-based node coordinates) get
- * sqrt(dx^2+dy^2+dz^2) * f[node] * h. */
-void orc_src_u0(const double* f, int m, int n, int l, double h, double sx,
-                double sy, double sz, double* u0);
+/* Near-source initial condition: u0 = 1000 everywhere, and the 8 nodes
+ * (i, j, k) around the fractional source (sx,sy,sz) (0-based node
+ * coordinates; ceil and floor of each) get a value from the distance
+ * r = sqrt(dx^2+dy^2+dz^2) (dx = sx - i, ...):
+ *   ORC_SRC_GENE_OBS  (a = slowness) r * a[ceil sx, ceil sy, k] * h: one
+ *                     slowness per depth plane, taken at the (ceil, ceil)
+ *                     column (scripts/gene_obs.jl:42-51);
+ *   ORC_SRC_INVERSION (a = velocity) r * h / a[i, j, k]
+ *                     (scripts/inversion.jl:52-60, with a = vel0);
+ *   ORC_SRC_NODE      (a = slowness) r * a[i, j, k] * h. */
+#define ORC_SRC_GENE_OBS 0
+#define ORC_SRC_INVERSION 1
+#define ORC_SRC_NODE 2
+void orc_src_u0(const double* a, int m, int n, int l, double h, double sx,
+                double sy, double sz, int mode, double* u0);
 
 /* Trilinear travel-time sample at a fractional node position, with the
  * branch structure of scripts/inversion.jl:64-95 (0-based).  If w is not
@@ -80,7 +89,10 @@ double orc_sample(const double* u, int m, int n, int l, double x, double y,
  *            marks a missing pick (inversion.jl:81)
  *   out:     misfit = sum w (t_obs - t_pred)^2; t_pred (same layout as t_obs);
  *            grad (concatenated fields, summed over solves); iters per solve
- *            (forward iterations executed).  u0 is treated as a constant
+ *            (forward iterations executed).  src_mode: the near-source rule
+ *            of orc_src_u0; src_model: its array (all fields, concatenated),
+ *            or NULL for the evaluation's own slowness (ORC_SRC_GENE_OBS and
+ *            ORC_SRC_NODE only).  u0 is treated as a constant
  *            input (inversion.jl builds it from vel0), so no gradient flows
  *            through the near-source initial values.
  * nthreads > 1 runs solves on that many POSIX threads; results do not depend
@@ -91,7 +103,8 @@ int orc_batch_misfit_grad(int n_fields, const int32_t* dims, const double* h,
                           const double* sta_xyz, int n_solves,
                           const int32_t* solve_field, const double* src_xyz,
                           const double* t_obs, const double* weight, double tol,
-                          int max_iter, int nthreads, double* misfit,
+                          int max_iter, int nthreads, int src_mode,
+                          const double* src_model, double* misfit,
                           double* t_pred, double* grad, int32_t* iters);
 
 #ifdef __cplusplus

@@ -57,14 +57,15 @@ def lib():
                                    C.c_int64, _ip64, _ip64, _dp, _dp]
         L.orc_assemble.restype = C.c_int64
         L.orc_src_u0.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
-                                 C.c_double, C.c_double, _dp]
+                                 C.c_double, C.c_double, C.c_int, _dp]
         L.orc_src_u0.restype = None
         L.orc_sample.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                  C.c_double, C.c_void_p, C.c_void_p]
         L.orc_sample.restype = C.c_double
         L.orc_batch_misfit_grad.argtypes = [C.c_int, _ip32, _dp, _dp, _ip32, _dp, C.c_int, _ip32,
                                             _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
-                                            C.POINTER(C.c_double), _dp, _dp, _ip32]
+                                            C.c_int, C.c_void_p, C.POINTER(C.c_double), _dp, _dp,
+                                            _ip32]
         L.orc_batch_misfit_grad.restype = C.c_int
         _LIB = L
     return _LIB
@@ -163,12 +164,22 @@ def assemble(dim, u, u0=None, ix=0, jx=0):
     return rows[:nt], cols[:nt], vals[:nt], mask
 
 
-def src_u0(f, h, src):
-    f = _c(f)
-    m, n, l = f.shape
-    u0 = np.empty_like(f)
-    lib().orc_src_u0(f.ravel(), m, n, l, float(h), float(src[0]), float(src[1]), float(src[2]),
-                     u0.ravel())
+SRC_MODES = {"gene_obs": 0, "inversion": 1, "node": 2}
+
+
+def src_u0(a, h, src, mode="gene_obs"):
+    """u0 = 1000 except the 8 nodes around the fractional 0-based source.
+
+    mode "gene_obs": a is the slowness; distance * a[ceil x, ceil y, k] * h
+        (scripts/gene_obs.jl:42-51: one slowness per depth plane);
+    mode "inversion": a is the velocity vel0; distance * h / a[node]
+        (scripts/inversion.jl:52-60);
+    mode "node": a is the slowness; distance * a[node] * h."""
+    a = _c(a)
+    m, n, l = a.shape
+    u0 = np.empty_like(a)
+    lib().orc_src_u0(a.ravel(), m, n, l, float(h), float(src[0]), float(src[1]), float(src[2]),
+                     SRC_MODES[mode], u0.ravel())
     return u0
 
 
@@ -183,11 +194,13 @@ def sample(u, xyz):
 
 
 def batch_misfit_grad(fields, stations, solve_field, src_xyz, t_obs, weight, tol=1e-6,
-                      max_iter=20, nthreads=1):
+                      max_iter=20, nthreads=1, src_mode="gene_obs", src_model=None):
     """FP64 misfit + summed slowness gradient over solves.
 
     fields: list of (slowness (m,n,l) array, h); stations: list of (S_f, 3) arrays.
     t_obs / weight: 1-D arrays, concatenated per solve (nsta of the solve's field).
+    src_mode / src_model: the near-source rule of src_u0 and its arrays (one
+    per field; None: the evaluation's own slowness, not for "inversion").
     Returns (misfit, t_pred, [grad per field], iters)."""
     dims = np.array([f.shape for f, _ in fields], np.int32).ravel()
     hs = np.array([h for _, h in fields], np.float64)
@@ -202,8 +215,12 @@ def batch_misfit_grad(fields, stations, solve_field, src_xyz, t_obs, weight, tol
     grad = np.empty_like(slow)
     iters = np.empty(len(sf), np.int32)
     mis = C.c_double(0.0)
+    model = (np.concatenate([_c(a).ravel() for a in src_model]) if src_model is not None
+             else None)
     rc = lib().orc_batch_misfit_grad(len(fields), dims, hs, slow, nsta, sta, len(sf), sf, src,
                                      t_obs, weight, float(tol), int(max_iter), int(nthreads),
+                                     SRC_MODES[src_mode],
+                                     model.ctypes.data if model is not None else None,
                                      C.byref(mis), t_pred, grad, iters)
     assert rc == 0
     out, off = [], 0

@@ -90,7 +90,7 @@ def main():
     # 3D: layered + checkerboard, fractional source, receivers on the top face
     m, n, l = 17, 13, 11
     f = layered_checker(m, n, l, 4)
-    u0 = O.src_u0(f, 1.0, (5.3, 7.6, 4.2))
+    u0 = O.src_u0(f, 1.0, (5.3, 7.6, 4.2), mode="node")
     gu = np.zeros((m, n, l))
     gu[:, :, 0] = rng.standard_normal((m, n))
     case3d("g3d_layered", u0, f, 1.0, 1e-6, gu)
@@ -118,7 +118,7 @@ def main():
     # convergence
     m, n, l = 40, 36, 20
     f = layered_checker(m, n, l, 8)
-    u0 = O.src_u0(f, 1.0, (20.5, 11.25, 9.75))
+    u0 = O.src_u0(f, 1.0, (20.5, 11.25, 9.75), mode="node")
     gu = np.zeros((m, n, l))
     gu[:, :, 0] = rng.standard_normal((m, n))
     case3d("g3d_layered_tol1e3", u0, f, 1.0, 1e-3, gu)

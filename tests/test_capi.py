@@ -95,7 +95,7 @@ def test_batch_null_handle_is_rejected():
     assert L.adt_batch_upload(None, None, None, None) == -1
     assert L.adt_batch_run_resident(None) == -1
     assert L.adt_batch_autotune(None, 1) == -1
-    assert L.adt_batch_set_source_slowness(None, None) == -1
+    assert L.adt_batch_set_source_velocity(None, None) == -1
     assert L.adt_batch_download(None, None, None, None, None) == -1
     assert L.adt_batch_run(None, one.ctypes.data_as(C.c_void_p), None, None, None, None, None,
                            None) == -1

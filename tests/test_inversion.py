@@ -112,30 +112,6 @@ def _small_problem(rng, shape=(24, 20, 14), h=0.5, nsta=6, neve=10):
 
 
 @pytest.mark.gpu
-def test_source_slowness_fixed_matches_oracle():
-    rng = np.random.default_rng(5)
-    m, n, l, h = 18, 16, 12, 0.5
-    s = synth.layered_checkerboard(m, n, l, block=4)
-    s0 = np.full_like(s, s.mean())
-    sta = synth.surface_stations(m, n, 5, rng)
-    src = synth.volume_sources(m, n, l, 3, rng)
-    P = A.Batch3D([(m, n, l, h)], [sta], np.zeros(3, np.int32), src, precision=A.ADT_F64,
-                  tol=1e-6, ref_compat=True)
-    A._lib.check(A.lib().adt_batch_set_source_slowness(P._h, s0.ctypes.data))
-    _, tp, _, _ = P.run([s], np.full(15, 1.0), np.ones(15))
-    for q in range(3):
-        u = O.eik3d_forward(O.src_u0(s0, h, src[q]), s, h, 1e-6)[0]
-        for k in range(5):
-            assert tp[q * 5 + k] == O.sample(u, sta[k])[0]
-    # back to the evaluation's own slowness
-    A._lib.check(A.lib().adt_batch_set_source_slowness(P._h, None))
-    _, tp2, _, _ = P.run([s], np.full(15, 1.0), np.ones(15))
-    u = O.eik3d_forward(O.src_u0(s, h, src[0]), s, h, 1e-6)[0]
-    assert tp2[0] == O.sample(u, sta[0])[0]
-    P.close()
-
-
-@pytest.mark.gpu
 def test_inversion_gradient_fd():
     rng = np.random.default_rng(6)
     grid, vel0, sta, eve, uobs, qua = _small_problem(rng)

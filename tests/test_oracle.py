@@ -13,6 +13,7 @@ import os
 import numpy as np
 import pytest
 
+from adtomo_gb300 import synth
 from oracle import oracle as O
 
 GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
@@ -155,3 +156,52 @@ def test_batch_matches_single_solves():
         g1 += O.eik3d_backward(gu, u, u0, f, h)[1]
     assert abs(mis - mis1) <= 1e-12 * mis1
     np.testing.assert_allclose(grads[0], g1, rtol=0, atol=1e-12 * np.abs(g1).max())
+
+
+def _julia_u0(a, h, ix, iy, iz, rule):
+    """Line-by-line restatement of the two Julia caller blocks on Julia's
+    1-based coordinates (ix, iy, iz): scripts/gene_obs.jl:39-51 (rule
+    "gene_obs", a = slowness) and scripts/inversion.jl:48-60 (rule
+    "inversion", a = vel0)."""
+    ixu, ixd = int(np.ceil(ix)), int(np.floor(ix))
+    iyu, iyd = int(np.ceil(iy)), int(np.floor(iy))
+    izu, izd = int(np.ceil(iz)), int(np.floor(iz))
+    u0 = 1000 * np.ones(a.shape)
+    A = lambda i, j, k: a[i - 1, j - 1, k - 1]  # noqa: E731  (1-based read)
+
+    def put(i, j, k, v):
+        u0[i - 1, j - 1, k - 1] = v
+
+    if rule == "gene_obs":
+        pu, pd = A(ixu, iyu, izu), A(ixu, iyu, izd)
+        for i in (ixu, ixd):
+            for j in (iyu, iyd):
+                for k, s in ((izu, pu), (izd, pd)):
+                    put(i, j, k, np.sqrt((ix - i) * (ix - i) + (iy - j) * (iy - j) +
+                                         (iz - k) * (iz - k)) * s * h)
+    else:
+        for i in (ixu, ixd):
+            for j in (iyu, iyd):
+                for k in (izu, izd):
+                    put(i, j, k, np.sqrt((ix - i) * (ix - i) + (iy - j) * (iy - j) +
+                                         (iz - k) * (iz - k)) * h / A(i, j, k))
+    return u0
+
+
+@pytest.mark.parametrize("src1", [(4.6, 8.3, 4.5), (12.25, 4.8, 8.1), (5.0, 7.0, 3.0),
+                                  (1.0, 1.3, 14.0), (20.0, 18.0, 1.75), (7.123456789, 9.87, 2.2)])
+def test_src_u0_rules_follow_the_reference_callers(src1):
+    """orc_src_u0 reproduces the caller code bit for bit: gene_obs.jl's one
+    slowness per depth plane from the (ceil x, ceil y) column, and
+    inversion.jl's h / vel0 per node (including integral coordinates and grid
+    edges).  The callers read 1-based coordinates; the library takes x - 1,
+    which is exact for x >= 1, so the distances are the same bits."""
+    m, n, l, h = 20, 18, 14, 0.5
+    f = synth.layered_checkerboard(m, n, l, block=4)
+    v0 = 1.0 / synth.layered_checkerboard(m, n, l, block=2)
+    src0 = tuple(x - 1.0 for x in src1)
+    assert all((x0 + 1.0) - 1.0 == x0 for x0 in src0)
+    assert np.array_equal(O.src_u0(f, h, src0, mode="gene_obs"),
+                          _julia_u0(f, h, *src1, "gene_obs"))
+    assert np.array_equal(O.src_u0(v0, h, src0, mode="inversion"),
+                          _julia_u0(v0, h, *src1, "inversion"))
