@@ -42,7 +42,8 @@ class BatchOpts(C.Structure):
                 ("adj_max_iter", C.c_int32), ("ref_compat", C.c_int32),
                 ("near_src_f64", C.c_int32), ("chunk", C.c_int32), ("bk", C.c_int32),
                 ("warps", C.c_int32), ("groups", C.c_int32), ("use_graph", C.c_int32),
-                ("wake_tol", C.c_double), ("adj_wake_tol", C.c_double)]
+                ("wake_tol", C.c_double), ("adj_wake_tol", C.c_double),
+                ("adj_order_filter", C.c_int32)]
 
 
 class BatchStats(C.Structure):

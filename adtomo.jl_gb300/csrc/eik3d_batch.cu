@@ -191,6 +191,7 @@ void batch_opts_default(adt_batch_opts* o) {
   o->use_graph = 1;
   o->wake_tol = 0.0;
   o->adj_wake_tol = 0.0;
+  o->adj_order_filter = 1;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -199,20 +200,20 @@ static int enqueue(BatchPlan& P, bool capturing);
 // many groups per CTA as shared memory, registers and `max_threads` allow
 // (at most `groups_req` when > 0); confirmed with the occupancy calculator.
 static int fit_shape(const void* fn, size_t warp_bytes, int regs, int max_threads, int meta_smem,
-                     int max_nb, size_t budget, int gw_req, int groups_req, int& gw, int& groups,
-                     size_t& smem) {
+                     int max_nb, int narr, size_t budget, int gw_req, int groups_req, int& gw,
+                     int& groups, size_t& smem) {
   const int max_warps = std::min(max_threads / 32, 65536 / std::max(1, regs * 32));
   gw = std::max(1, std::min(gw_req, max_warps));
   for (;;) {
     int G = 1;
     while (G < 15 &&
-           group_hdr_bytes(G + 1, meta_smem, max_nb) + (size_t)(G + 1) * gw * warp_bytes <= budget &&
+           group_hdr_bytes(G + 1, meta_smem, max_nb, narr) + (size_t)(G + 1) * gw * warp_bytes <= budget &&
            (G + 1) * gw <= max_warps)
       ++G;
-    if (group_hdr_bytes(G, meta_smem, max_nb) + (size_t)G * gw * warp_bytes <= budget) {
+    if (group_hdr_bytes(G, meta_smem, max_nb, narr) + (size_t)G * gw * warp_bytes <= budget) {
       if (groups_req > 0) G = std::min(G, groups_req);
       for (; G >= 1; --G) {  // shrink until one CTA fits
-        smem = group_hdr_bytes(G, meta_smem, max_nb) + (size_t)G * gw * warp_bytes;
+        smem = group_hdr_bytes(G, meta_smem, max_nb, narr) + (size_t)G * gw * warp_bytes;
         ADT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int occ = 0;
         ADT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, G * gw * 32, smem));
@@ -237,11 +238,11 @@ static int fit_shape(const void* fn, size_t warp_bytes, int regs, int max_thread
 static int apply_shapes(BatchPlan* P, int fwd_gw, int fwd_groups, int adj_gw, int adj_groups) {
   int rc;
   if ((rc = fit_shape(P->ks.fwd, P->fwd_wbytes, P->fwd_regs, ADT_FWD_MAXT, P->meta_smem, P->max_nb,
-                      P->smem_budget, fwd_gw > 0 ? fwd_gw : (P->f64 ? 2 : 6), fwd_groups,
+                      META_ARRAYS_FWD, P->smem_budget, fwd_gw > 0 ? fwd_gw : (P->f64 ? 2 : 6), fwd_groups,
                       P->fwd_gw, P->fwd_groups, P->fwd_smem)))
     return rc;
   if ((rc = fit_shape(P->ks.adj, P->adj_wbytes, P->adj_regs, 1024, P->meta_smem, P->max_nb,
-                      P->smem_budget, adj_gw > 0 ? adj_gw : (P->f64 ? 2 : 4), adj_groups,
+                      META_ARRAYS_ADJ, P->smem_budget, adj_gw > 0 ? adj_gw : (P->f64 ? 2 : 4), adj_groups,
                       P->adj_gw, P->adj_groups, P->adj_smem)))
     return rc;
   P->fwd_warps = P->fwd_gw * P->fwd_groups;
@@ -381,7 +382,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       P->solves[s].seed_off = seeds;
       ch.field_uoff[P->solve_field[s]].push_back(cells);
       cells += (g.ncell + 15) / 16 * 16;  // 64-byte aligned solves: the FP32 path uses 16-byte accesses
-      bricks += (int64_t)META_ARRAYS * g.nbx * g.nby * g.nbz;
+      bricks += (int64_t)META_ARRAYS_MAX * g.nbx * g.nby * g.nbz;
       seeds += 8LL * P->nsta[P->solve_field[s]];
     }
     max_cells = std::max(max_cells, cells);
@@ -517,7 +518,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   P->fwd_wbytes = P->f64 ? fwd_warp_smem<double>(P->bk) : fwd_warp_smem<float>(P->bk);
   P->adj_wbytes = P->f64 ? adj_warp_smem<double>(P->bk) : adj_warp_smem<float>(P->bk);
   for (auto& g : P->geoms) P->max_nb = std::max(P->max_nb, g.nbx * g.nby * g.nbz);
-  P->meta_smem = ((size_t)META_ARRAYS * P->max_nb * sizeof(int) <= 16384) ? 1 : 0;
+  P->meta_smem = ((size_t)META_ARRAYS_MAX * P->max_nb * sizeof(int) <= 16384) ? 1 : 0;
   {
     cudaFuncAttributes fa_f, fa_a;
     ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
@@ -585,6 +586,7 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.group_warps = which_counter % 2 == 0 ? P.fwd_gw : P.adj_gw;
   A.meta_smem = P.meta_smem;
   A.max_nb = P.max_nb;
+  A.adj_order_filter = P.opts.adj_order_filter ? 1 : 0;
   return A;
 }
 

@@ -83,6 +83,7 @@ struct BatchArgs {
   int group_warps;          // warps per group (one solve per group)
   int meta_smem;            // 1: brick meta of the running solve in shared memory
   int max_nb;               // bricks of the largest field (shared-memory meta size)
+  int adj_order_filter;     // 1: adjoint sweeps a brick only in the orderings its flow allows
 };
 
 // Per-group scalars at the start of dynamic shared memory.
@@ -96,14 +97,19 @@ __device__ __forceinline__ void group_sync(int grp, int nthreads) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(grp + 1), "r"(nthreads) : "memory");
 }
 
-// Brick metadata of one solve: two arrays of one int per brick, mod and proc
-// (timestamps of the last change and of the last sweep).
-constexpr int META_ARRAYS = 2;
+// Brick metadata of one solve: arrays of one int per brick.  Both sweeps keep
+// mod and proc (timestamps of the last change and of the last sweep); the
+// adjoint adds flow (the directions in which adjoint values enter the
+// brick's cells, which orderings it is swept in).  The global meta buffer
+// holds META_ARRAYS_MAX arrays per solve.
+constexpr int META_ARRAYS_FWD = 2;
+constexpr int META_ARRAYS_ADJ = 3;
+constexpr int META_ARRAYS_MAX = 3;
 
-// Dynamic shared memory: [G GroupShared][G * 2 * max_nb meta ints][warp tiles]
-__host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_nb) {
+// Dynamic shared memory: [G GroupShared][G * narr * max_nb meta ints][warp tiles]
+__host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_nb, int narr) {
   size_t b = ((size_t)G * sizeof(GroupShared) + 15) / 16 * 16;
-  if (meta_smem) b += ((size_t)G * META_ARRAYS * max_nb * sizeof(int) + 15) / 16 * 16;
+  if (meta_smem) b += ((size_t)G * narr * max_nb * sizeof(int) + 15) / 16 * 16;
   return b;
 }
 
@@ -151,21 +157,49 @@ __device__ __forceinline__ double from_ordered<double>(unsigned long long b) {
 // proc = t, then mod = t if something changed.  A reader sees either the old
 // words (dirty, as the sweeper found), proc == t (dirty by the first test) or
 // the old proc with mod == t (dirty by the second), so the answer is the same.
+//
+// feeds: which face neighbours can change the brick's values (bit 0: x-,
+// 1: x+, 2: y-, 3: y+, 4: z-, 5: z+); 63 for the forward, where any
+// neighbour may become a cell's upwind neighbour.  The adjoint passes its
+// flow bits: a brick none of whose cells is used by a cell across a face
+// reads that face's adjoint values only with zero weight, so a change there
+// cannot change the brick.
 __device__ __forceinline__ bool brick_dirty(const int* mod_, const int* proc_, const Geom& g,
-                                            int b, int bx, int by, int bz, int t) {
+                                            int b, int bx, int by, int bz, int t, int feeds = 63) {
   const volatile int* mod = mod_;
   const volatile int* proc = proc_;
   const int pr = proc[b];
   if (pr == t) return true;
   bool v = mod[b] >= pr;
   const int sx = g.nby * g.nbz;
-  if (bx > 0) v |= mod[b - sx] > pr;
-  if (bx < g.nbx - 1) v |= mod[b + sx] > pr;
-  if (by > 0) v |= mod[b - g.nbz] > pr;
-  if (by < g.nby - 1) v |= mod[b + g.nbz] > pr;
-  if (bz > 0) v |= mod[b - 1] > pr;
-  if (bz < g.nbz - 1) v |= mod[b + 1] > pr;
+  if ((feeds & 1) && bx > 0) v |= mod[b - sx] > pr;
+  if ((feeds & 2) && bx < g.nbx - 1) v |= mod[b + sx] > pr;
+  if ((feeds & 4) && by > 0) v |= mod[b - g.nbz] > pr;
+  if ((feeds & 8) && by < g.nby - 1) v |= mod[b + g.nbz] > pr;
+  if ((feeds & 16) && bz > 0) v |= mod[b - 1] > pr;
+  if ((feeds & 32) && bz < g.nbz - 1) v |= mod[b + 1] > pr;
   return v;
+}
+
+// Orderings of the adjoint sweeps that follow a brick's flow.  The adjoint
+// system is triangular: lambda flows from a cell to its upwind neighbour
+// (from user r to c), so a sweep carries it within one pass only when it
+// visits r before c.  flow holds the user bits of the brick's cells, OR-ed
+// (bit 0: the x- neighbour uses a cell, so lambda flows along +x and needs an
+// ordering with si = +1; bit 1: along -x, si = -1; bits 2-3 y, 4-5 z).  An
+// ordering is kept when it agrees with every axis whose flow has one
+// direction; an axis with both directions (or none) constrains nothing.
+// Skipping the other orderings is exact: a skipped dirty brick stays dirty
+// (its timestamps do not move) and is swept in an allowed ordering of the
+// same or the next iteration, and the solve stops only after an iteration in
+// which nothing changed, so at the end every cell satisfies its equation --
+// and the triangular system has exactly one such solution.
+__host__ __device__ __forceinline__ int adjoint_flow_forbidden(int si, int sj, int sk) {
+  return (si > 0 ? 2 : 1) | (sj > 0 ? 8 : 4) | (sk > 0 ? 32 : 16);
+}
+__host__ __device__ __forceinline__ bool adjoint_flow_allowed(int flow, int forbid) {
+  const int both = flow & (flow >> 1) & 0x15;
+  return ((flow & ~(both | (both << 1))) & forbid) == 0;
 }
 
 // ------------------------------------------------------------------ forward
@@ -173,12 +207,13 @@ __device__ __forceinline__ bool brick_dirty(const int* mod_, const int* proc_, c
 struct GroupCtx {
   int NW, GW, G, warp, lane, grp, gw, gthreads;
   GroupShared* gs;
-  int* smeta;  // this group's meta (META_ARRAYS * max_nb ints) or null
+  int* smeta;  // this group's meta (narr * max_nb ints) or null
   unsigned char* tiles;
 };
 
 template <class T>
-__device__ __forceinline__ GroupCtx group_ctx(const BatchArgs<T>& A, unsigned char* smem) {
+__device__ __forceinline__ GroupCtx group_ctx(const BatchArgs<T>& A, unsigned char* smem,
+                                              int narr) {
   GroupCtx c;
   c.NW = blockDim.x >> 5;
   c.GW = A.group_warps;
@@ -191,9 +226,9 @@ __device__ __forceinline__ GroupCtx group_ctx(const BatchArgs<T>& A, unsigned ch
   c.gs = reinterpret_cast<GroupShared*>(smem) + c.grp;
   const size_t g0 = ((size_t)c.G * sizeof(GroupShared) + 15) / 16 * 16;
   c.smeta = A.meta_smem
-                ? reinterpret_cast<int*>(smem + g0) + (size_t)c.grp * META_ARRAYS * A.max_nb
+                ? reinterpret_cast<int*>(smem + g0) + (size_t)c.grp * narr * A.max_nb
                 : nullptr;
-  c.tiles = smem + group_hdr_bytes(c.G, A.meta_smem, A.max_nb);
+  c.tiles = smem + group_hdr_bytes(c.G, A.meta_smem, A.max_nb, narr);
   return c;
 }
 
@@ -238,13 +273,21 @@ __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx&
 //
 // body(p) sweeps one dirty brick and returns whether it changed; this
 // function keeps the brick's timestamps (t = ts0 + level) and counters.
+//
+// flow (adjoint only, else null): per brick, the directions in which adjoint
+// values enter its cells (user bits of adjoint_flow_allowed); a dirty brick
+// is swept only in the orderings that follow them, and only changes of the
+// face neighbours that feed it make it dirty (brick_dirty).  flow is written
+// before the sweeps and not during them, so every warp still reads the same
+// mask.
 template <int BK, class Body>
 __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, const uint32_t* bricks,
-                                             const int* lstart, int* mod, int* proc, int ts0,
-                                             int si, int sj, int sk,
+                                             const int* lstart, int* mod, int* proc,
+                                             const int* flow, int ts0, int si, int sj, int sk,
                                              unsigned long long& cnt_upd,
                                              unsigned long long& cnt_brk, Body&& body) {
   const int lane = c.lane;
+  const int forbid = flow ? adjoint_flow_forbidden(si, sj, sk) : 0;
   for (int d = 0; d < g.nlev; ++d) {
     const int t = ts0 + d;
     const int q0 = lstart[d], q1 = lstart[d + 1];
@@ -260,7 +303,13 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
         const int bx = si > 0 ? rx : g.nbx - 1 - rx;
         const int by = sj > 0 ? ry : g.nby - 1 - ry;
         const int bz = sk > 0 ? rz : g.nbz - 1 - rz;
-        dv = brick_dirty(mod, proc, g, (bx * g.nby + by) * g.nbz + bz, bx, by, bz, t);
+        const int b = (bx * g.nby + by) * g.nbz + bz;
+        if (flow) {
+          const int fl = ((const volatile int*)flow)[b];
+          dv = adjoint_flow_allowed(fl, forbid) && brick_dirty(mod, proc, g, b, bx, by, bz, t, fl);
+        } else {
+          dv = brick_dirty(mod, proc, g, b, bx, by, bz, t);
+        }
       }
       unsigned m = __ballot_sync(0xffffffffu, dv);
       while (m) {
@@ -316,7 +365,7 @@ __device__ __forceinline__ bool dispatch_fwd_f32(float* S, const float* F, const
 template <class T, int BK, int MODE>
 __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const GroupCtx c = group_ctx(A, smem);
+  const GroupCtx c = group_ctx(A, smem, META_ARRAYS_FWD);
   if (c.grp >= c.G) return;
   const int lane = c.lane;
   T* S = reinterpret_cast<T*>(c.tiles) + c.warp * (tile_elems(BK) + itile_elems(BK));
@@ -382,8 +431,8 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
         int si, sj, sk;
         ordering3(o, si, sj, sk);
         const int CS = tile_col_stride(BK, sj == sk);
-        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, (it * 8 + o) * g.nlev, si, sj, sk,
-                         cnt_upd, cnt_brk, [&](const BrickPos& p) -> bool {
+        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, nullptr, (it * 8 + o) * g.nlev,
+                         si, sj, sk, cnt_upd, cnt_brk, [&](const BrickPos& p) -> bool {
           bool ch;
           if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
             if (vec) {
@@ -667,9 +716,9 @@ __device__ __forceinline__ void adj_pass1_vec4(const float* u, uint16_t* code, f
 
 // User bits of four consecutive cells (pass 2) from 8-byte loads of the
 // codes: neighbour r uses c when r is not fixed and its upwind side along
-// the axis points at c.
-__device__ __forceinline__ void adj_pass2_vec4(uint16_t* code, const Geom& g, int64_t x, int i,
-                                               int j, int k) {
+// the axis points at c.  Returns the OR of the four cells' user bits.
+__device__ __forceinline__ uint32_t adj_pass2_vec4(uint16_t* code, const Geom& g, int64_t x,
+                                                   int i, int j, int k) {
   const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
   auto ld4 = [&](int64_t y) -> uint2 { return *reinterpret_cast<const uint2*>(code + y); };
   auto c16 = [](uint2 v, int q) -> uint32_t {
@@ -687,6 +736,7 @@ __device__ __forceinline__ void adj_pass2_vec4(uint16_t* code, const Geom& g, in
     return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
   };
   uint32_t packed[2] = {0u, 0u};
+  uint32_t all = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     uint32_t cd = c16(c4, q);
@@ -699,10 +749,12 @@ __device__ __forceinline__ void adj_pass2_vec4(uint16_t* code, const Geom& g, in
       if (uses(q == 0 ? zm : c16(c4, q - 1), 2, 2u)) us |= 16u;
       if (uses(q == 3 ? zp : c16(c4, q + 1), 2, 1u)) us |= 32u;
       cd |= us << CODE_USERS;
+      all |= us;
     }
     packed[q >> 1] |= cd << (16 * (q & 1));
   }
   *reinterpret_cast<uint2*>(code + x) = make_uint2(packed[0], packed[1]);
+  return all;
 }
 
 template <int BK>
@@ -729,7 +781,7 @@ __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const
 template <class T, int BK>
 __global__ void k_batch_adj(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const GroupCtx c = group_ctx(A, smem);
+  const GroupCtx c = group_ctx(A, smem, META_ARRAYS_ADJ);
   if (c.grp >= c.G) return;
   const int lane = c.lane;
   constexpr size_t WS = (2 * tile_elems(BK)) * sizeof(T) + itile_elems(BK) * sizeof(uint16_t);
@@ -753,6 +805,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     const int nb = g.nbx * g.nby * g.nbz;
     int* mod = c.smeta ? c.smeta : A.meta + sd.meta_off;
     int* proc = mod + (c.smeta ? A.max_nb : nb);
+    int* flow = proc + (c.smeta ? A.max_nb : nb);
     const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
     const bool vec = (g.l % 8) == 0;
     // pass 1: upwind sides and fixed cells; lambda = 0
@@ -782,15 +835,22 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
       mod[b] = -2;
       proc[b] = -1;
+      flow[b] = 0;
     }
     group_sync(c.grp, c.gthreads);
-    // pass 2: users (reads only the low bits of neighbours, writes own high bits)
+    // pass 2: users (reads only the low bits of neighbours, writes own high bits);
+    // each brick's flow collects its cells' user bits
+    auto add_flow = [&](int i, int j, int k, uint32_t us) {
+      if (!us) return;
+      int* fb = flow + ((i / BI) * g.nby + (j / BJ)) * g.nbz + (k / BK);
+      if ((((const volatile int*)fb)[0] & (int)us) != (int)us) atomicOr(fb, (int)us);
+    };
     if constexpr (sizeof(T) == 4) {
       if (vec4)
         for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += c.gthreads) {
           const int64_t col = e / (g.l / 4);
-          adj_pass2_vec4(code, g, 4 * e, (int)(col / g.n), (int)(col % g.n),
-                         (int)(4 * e - col * g.l));
+          const int i = (int)(col / g.n), j = (int)(col % g.n), k = (int)(4 * e - col * g.l);
+          add_flow(i, j, k, adj_pass2_vec4(code, g, 4 * e, i, j, k));
         }
     }
     for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
@@ -811,6 +871,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         if (k > 0 && uses(x - 1, 2, 2)) us |= 16;
         if (k < g.l - 1 && uses(x + 1, 2, 1)) us |= 32;
         code[x] = (uint16_t)(cd | (us << CODE_USERS));
+        add_flow(i, j, k, us);
       }
     }
     group_sync(c.grp, c.gthreads);
@@ -837,8 +898,9 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         int si, sj, sk;
         ordering3(o, si, sj, sk);
         const int CS = tile_col_stride(BK, sj == sk);
-        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, (it * 8 + o) * g.nlev, si, sj, sk,
-                         cnt_upd, cnt_brk, [&](const BrickPos& p) -> bool {
+        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, A.adj_order_filter ? flow : nullptr,
+                         (it * 8 + o) * g.nlev, si, sj, sk, cnt_upd, cnt_brk,
+                         [&](const BrickPos& p) -> bool {
           bool ch;
           if constexpr (sizeof(T) == 4) {
             if (vec) {

@@ -56,6 +56,29 @@ def workload():
     return f, f_obs, sta, src, w
 
 
+def sample_weights(sta, m=M, n=N, l=L):
+    """Node indices and trilinear weights of each station (scripts/inversion.jl:64-95:
+    floor/ceil per axis, weight 1 on an axis where they agree), for the host-side
+    misfit of the plain single-event path."""
+    idx = np.zeros((len(sta), 8), np.int64)
+    wt = np.zeros((len(sta), 8))
+    for q, (x, y, z) in enumerate(sta):
+        xi = (int(np.floor(x)), int(np.ceil(x)))
+        yi = (int(np.floor(y)), int(np.ceil(y)))
+        zi = (int(np.floor(z)), int(np.ceil(z)))
+        xw = (1.0, 0.0) if xi[0] == xi[1] else (xi[1] - x, x - xi[0])
+        yw = (1.0, 0.0) if yi[0] == yi[1] else (yi[1] - y, y - yi[0])
+        zw = (1.0, 0.0) if zi[0] == zi[1] else (zi[1] - z, z - zi[0])
+        c = 0
+        for a in range(2):
+            for b in range(2):
+                for d in range(2):
+                    idx[q, c] = (xi[a] * n + yi[b]) * l + zi[d]
+                    wt[q, c] = xw[a] * yw[b] * zw[d]
+                    c += 1
+    return idx, wt
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -116,38 +139,105 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons)}
 
 
-def cpu_events_per_s(sample_events, threads):
-    """The oracle port of the reference's CPU op on a bounded sample."""
+def oracle_picks(k):
+    """Observed times of the first k events: the reference's FP64 op (the
+    oracle port, tol 1e-6, 20-iteration cap) on the +2%-noise model, sampled at
+    the stations.  The same bits as the GPU arm's picks, which come from the
+    library's FP64 plan with the reference stopping rule (bit-exact to the
+    oracle).  Untimed setup of the CPU legs."""
+    from oracle import oracle as O
+    f, f_obs, sta, src, w = workload()
+    threads = os.cpu_count() or 1
+    _, tp, _, _ = O.batch_misfit_grad([(f_obs, H)], [sta], np.zeros(k, np.int32), src[:k],
+                                      np.full(k * N_STA, 1.0), w[:k * N_STA], tol=1e-6,
+                                      max_iter=20, nthreads=threads)
+    return tp
+
+
+def cpu_events_per_s(sample_events, threads, t_obs):
+    """The oracle port of the reference's CPU op on a bounded sample, with the
+    given picks (t_obs of the first sample_events events).  Returns
+    (events/s, seconds, (misfit, t_pred, grad))."""
     from oracle import oracle as O
     f, f_obs, sta, src, w = workload()
     k = sample_events
-    t_obs = np.full(k * N_STA, 1.0)
     t0 = time.perf_counter()
-    O.batch_misfit_grad([(f, H)], [sta], np.zeros(k, np.int32), src[:k], t_obs, w[:k * N_STA],
-                        tol=1e-6, max_iter=20, nthreads=threads)
+    mis, tp, (g,), _ = O.batch_misfit_grad([(f, H)], [sta], np.zeros(k, np.int32), src[:k],
+                                           t_obs[:k * N_STA], w[:k * N_STA], tol=1e-6,
+                                           max_iter=20, nthreads=threads)
     dt = time.perf_counter() - t0
-    return k / dt, dt
+    return k / dt, dt, (mis, tp, g)
 
 
-def plain_fp64_events_per_s(k):
+def plain_fp64_events_per_s(k, t_obs):
     """The plain FP64 single-event GPU path on the same workload: one event
     per call (adt_eikonal_three_d, then adt_eikonal_three_d_grad), no
-    batching, no graph; misfit sampling and seeds on the host."""
+    batching, no graph.  u0 (scripts/gene_obs.jl:42-51's near-source rule, in
+    NumPy) and the stations' trilinear weights are built before the timer;
+    inside it only the two library calls and the host-side misfit seeds (a
+    NumPy gather and scatter).  Picks t_obs as in the batched legs."""
     import adtomo_gb300 as A
-    from oracle import oracle as O
     f, f_obs, sta, src, w = workload()
-    t_obs = np.full(N_STA, 1.0)
+    idx, wt = sample_weights(sta)
+    u0s = []
+    for e in range(k):
+        u0 = np.full(M * N * L, 1000.0)
+        xs = (int(np.ceil(src[e, 0])), int(np.floor(src[e, 0])))
+        ys = (int(np.ceil(src[e, 1])), int(np.floor(src[e, 1])))
+        zs = (int(np.ceil(src[e, 2])), int(np.floor(src[e, 2])))
+        fcol = f[xs[0], ys[0]]
+        for a in xs:
+            for b in ys:
+                for c in zs:
+                    r = np.sqrt((src[e, 0] - a) ** 2 + (src[e, 1] - b) ** 2 + (src[e, 2] - c) ** 2)
+                    u0[(a * N + b) * L + c] = r * fcol[c] * H
+        u0s.append(u0.reshape(M, N, L))
     t0 = time.perf_counter()
     for e in range(k):
-        u0 = O.src_u0(f, H, src[e])
-        u = A.eikonal3d(u0, f, H, M, N, L, 1e-6)
-        gu = np.zeros_like(u)
-        for q in range(N_STA):
-            t, idx, wt = O.sample(u, sta[q])
-            np.add.at(gu.ravel(), idx, -2.0 * (t_obs[q] - t) * wt)
-        A.eikonal3d_grad(gu, u, u0, f, H, M, N, L)
+        u = A.eikonal3d(u0s[e], f, H, M, N, L, 1e-6)
+        t = (u.ravel()[idx] * wt).sum(axis=1)
+        dt = -2.0 * w[e * N_STA:(e + 1) * N_STA] * (t_obs[e * N_STA:(e + 1) * N_STA] - t)
+        gu = np.bincount(idx.ravel(), weights=(dt[:, None] * wt).ravel(), minlength=M * N * L)
+        A.eikonal3d_grad(gu.reshape(M, N, L), u, u0s[e], f, H, M, N, L)
     dt = time.perf_counter() - t0
     return k / dt, dt
+
+
+def gpu_picks(A):
+    """Observed times of all events on the GPU: the library's FP64 plan with
+    the reference stopping rule (tol 1e-6, 20 iterations; bit-exact to the
+    reference's op) on the +2%-noise model.  Untimed setup."""
+    f, f_obs, sta, src, w = workload()
+    P = A.Batch3D([(M, N, L, H)], [sta], np.zeros(N_EVENTS, np.int32), src, precision=A.ADT_F64,
+                  tol=1e-6, ref_compat=True)
+    _, tp, _, _ = P.run([f_obs], np.full(N_EVENTS * N_STA, 1.0), w)
+    P.close()
+    return tp
+
+
+def fp64_batched_events_per_s(A, t_obs, steps=1):
+    """The same batched plan in FP64 (exact brick skipping, tol 1e-6): the
+    yardstick the FP32 path is measured against.  CUDA events around `steps`
+    evaluations after one warm-up."""
+    import torch
+    f, f_obs, sta, src, w = workload()
+    P = A.Batch3D([(M, N, L, H)], [sta], np.zeros(N_EVENTS, np.int32), src, precision=A.ADT_F64,
+                  tol=1e-6)
+    P.upload([f], t_obs, w)
+    P.run_resident()
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(P.stream())
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(steps):
+            P.run_resident()
+        end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    st = P.stats()
+    P.close()
+    return N_EVENTS / (ms / 1000.0), ms, st
 
 
 def run_reference(args, rank, world):
@@ -155,11 +245,12 @@ def run_reference(args, rank, world):
         return
     threads = os.cpu_count() or 1
     sample = max(threads, 16)
+    t_obs = oracle_picks(sample)  # untimed setup: the same picks as the GPU arm's
     for _ in range(args.warmup):
-        cpu_events_per_s(min(sample, threads), threads)
+        cpu_events_per_s(min(sample, threads), threads, t_obs)
     vals, total = [], 0.0
     for _ in range(args.steps):
-        v, dt = cpu_events_per_s(sample, threads)
+        v, dt, _ = cpu_events_per_s(sample, threads, t_obs)
         vals.append(v)
         total += dt
     value = sample * args.steps / total
@@ -169,7 +260,9 @@ def run_reference(args, rank, world):
         "ms_per_step": 1000.0 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "C3: 256 events on 128x128x64, h=0.5 km, layered+checkerboard, "
-                               "100 surface stations", "sample_events_per_step": sample},
+                               "100 surface stations", "sample_events_per_step": sample,
+                   "picks": "FP64 travel times on the +2%-noise model (reference stopping rule), "
+                            "the same bits as the GPU arm's"},
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} of the 256 events per step (oracle/eikonal_oracle.c, "
                                    f"FP64, tol 1e-6, 20-iteration cap, {threads} threads)"},
@@ -187,13 +280,11 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     f, f_obs, sta, src, w = workload()
     sf = np.zeros(N_EVENTS, np.int32)
+    # observed times: FP64 on the +2% noise model, reference stopping rule (setup, untimed)
+    t_obs = gpu_picks(A)
     B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
                   warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
                   adj_wake_tol=args.adj_wake_tol)
-    # observed times from the +2% noise model (setup, untimed)
-    B.upload([f_obs], np.full(N_EVENTS * N_STA, 1.0), w)
-    B.run_resident()
-    _, t_obs, _, _ = B.download()
     B.upload([f], t_obs, w)
     if args.autotune and not (args.warps or args.groups):
         B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
@@ -280,10 +371,41 @@ def run_ours(args, rank, world):
     d2h = 8 + n_obs * 8 + M * N * L * 8 + N_EVENTS * 24
     threads = os.cpu_count() or 1
     cpu_sample = max(threads, 16) if args.cpu_sample is None else args.cpu_sample
-    cpu_val, cpu_dt = (cpu_events_per_s(cpu_sample, threads) if cpu_sample > 0 else (None, 0.0))
+    cpu_sample = min(cpu_sample, N_EVENTS)
+    cpu_val, cpu_dt, cpu_out = (cpu_events_per_s(cpu_sample, threads, t_obs) if cpu_sample > 0
+                                else (None, 0.0, None))
+    err64 = None
+    if cpu_out is not None:
+        # FP32 error against the reference's FP64 op on the CPU sample: the same
+        # events, picks and options as the headline plan (untimed)
+        k = cpu_sample
+        E = A.Batch3D([(M, N, L, H)], [sta], np.zeros(k, np.int32), src[:k], precision=A.ADT_F32,
+                      tol=1e-6, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol)
+        mis_k, tp_k, (g_k,), _ = E.run([f], t_obs[:k * N_STA], w[:k * N_STA])
+        E.close()
+        mo, tpo, go = cpu_out
+        err64 = {"sample": f"first {k} events, all {N_STA} stations",
+                 "reference": "oracle port of Eikonal3D.cpp (FP64, tol 1e-6, 20-iteration cap, "
+                              "exact causal adjoint)",
+                 "t_pred_max_rel": float(np.max(np.abs(tp_k - tpo) / np.abs(tpo))),
+                 "t_pred_max_rel_in_headline_run": float(np.max(np.abs(tp[:k * N_STA] - tpo) /
+                                                               np.abs(tpo))),
+                 "misfit_rel": float(abs(mis_k - mo) / abs(mo)),
+                 "grad_rel_l2": float(np.linalg.norm(g_k - go) / np.linalg.norm(go)),
+                 "grad_max_abs_rel": float(np.max(np.abs(g_k - go)) / np.max(np.abs(go))),
+                 "tolerances": {"t_pred": 1e-4, "grad": 1e-3}}
     iters = [s.iters for s in status]
-    plain_val, plain_dt = (plain_fp64_events_per_s(args.plain_sample) if args.plain_sample > 0
-                           else (None, 0.0))
+    plain_val, plain_dt = (plain_fp64_events_per_s(args.plain_sample, t_obs)
+                           if args.plain_sample > 0 else (None, 0.0))
+    f64b = None
+    if args.fp64_batched:
+        v64, ms64, st64 = fp64_batched_events_per_s(A, t_obs)
+        f64b = {"value": v64, "unit": "events/s", "ms_per_evaluation": ms64,
+                "fwd_ms": st64.fwd_ms, "adj_ms": st64.adj_ms,
+                "cell_updates": int(st64.fwd_cell_updates + st64.adj_cell_updates),
+                "fp32_over_fp64": value / world / v64,
+                "what": "the same batched plan in FP64 (exact brick skipping, tol 1e-6), "
+                        "256 events, one evaluation after a warm-up, CUDA events"}
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -302,7 +424,8 @@ def run_ours(args, rank, world):
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
                    "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
-                   "vs_exact_skipping": vs_exact},
+                   "picks": "FP64 travel times on the +2%-noise model (reference stopping rule)",
+                   "vs_exact_skipping": vs_exact, "error_vs_fp64": err64},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -320,6 +443,7 @@ def run_ours(args, rank, world):
                         "sample": f"{args.plain_sample} events, one per call through "
                                   f"adt_eikonal_three_d + adt_eikonal_three_d_grad (FP64, "
                                   f"host buffers), {plain_dt:.2f} s"} if plain_val else None),
+        "fp64_batched": f64b,
         "clocks": clocks,
         # per evaluation of the one-field, one-chunk plan: k_to_t_f32, k_src_init,
         # k_batch_fwd, k_batch_misfit, k_batch_adj, k_batch_grad, k_grad_scale,
@@ -405,6 +529,90 @@ def run_large(args):
     B.close()
 
 
+def run_single(args):
+    """Secondary lines for the plain FP64 configurations (one event, no
+    batching), GPU through the host-pointer API against the oracle port of the
+    reference's CPU op on one core, with parity:
+      c1: 2D 101x101, h = 1 km, 6 km/s + 3 Gaussian anomalies (+-10%, sigma 8
+          cells), 1 interior source, 20 receivers at random nodes, misfit
+          against times from a +2%-noise model; 2D stopping rule (1e-8);
+      c2: 3D 64x64x32, h = 1 km, layered 4-8 km/s x (1+-5%) checkerboard of
+          8-cell blocks, 1 interior source, 50 surface receivers, tol 1e-6,
+          20-iteration cap."""
+    import adtomo_gb300 as A
+    from adtomo_gb300 import synth
+    from oracle import oracle as O
+    rng = np.random.default_rng(SEED)
+    if args.workload == "c1":
+        n1 = m1 = 101
+        f = 1.0 / synth.gaussian_anomalies_2d(n1, m1, rng)
+        f_obs = f / (1.0 + 0.02 * rng.standard_normal(f.shape))
+        ix, jx = (int(x) for x in rng.integers(1, m1 - 1, 2))  # 0-based source node
+        rx, ry = rng.integers(0, m1, 20), rng.integers(0, n1, 20)
+        t_obs = A.eikonal(f_obs, ix + 1, jx + 1, 1.0)[ry, rx]
+
+        def gpu():
+            u = A.eikonal(f, ix + 1, jx + 1, 1.0)
+            gu = np.zeros_like(u)
+            np.add.at(gu, (ry, rx), -2.0 * (t_obs - u[ry, rx]))
+            return u, A.eikonal_grad(gu, u, f, ix + 1, jx + 1, 1.0), gu
+
+        def cpu(gu):
+            u, _, _ = O.eik2d_forward(f, ix, jx, 1.0)
+            return u, O.eik2d_backward(gu, u, f, ix, jx, 1.0)
+        desc = ("C1: 2D 101x101, h=1 km, 6 km/s + 3 Gaussian anomalies (+-10%, sigma 8 cells), "
+                "1 interior source, 20 receivers, +2%-noise picks, stopping rule 1e-8")
+    else:
+        m, n, l, h = 64, 64, 32, 1.0
+        f = synth.layered_checkerboard(m, n, l, block=8)
+        src = synth.volume_sources(m, n, l, 1, rng)[0]
+        sta = synth.surface_stations(m, n, 50, rng)
+        idx, wt = sample_weights(sta, m, n, l)
+        f_obs = f * (1 + 0.02 * rng.standard_normal(f.shape))
+        u0 = O.src_u0(f, h, src)
+        uo = A.eikonal3d(O.src_u0(f_obs, h, src), f_obs, h, m, n, l, 1e-6)
+        t_obs = (uo.ravel()[idx] * wt).sum(axis=1)
+
+        def seeds(u):
+            t = (u.ravel()[idx] * wt).sum(axis=1)
+            dt = -2.0 * (t_obs - t)
+            return np.bincount(idx.ravel(), weights=(dt[:, None] * wt).ravel(),
+                               minlength=m * n * l).reshape(m, n, l)
+
+        def gpu():
+            u = A.eikonal3d(u0, f, h, m, n, l, 1e-6)
+            gu = seeds(u)
+            return u, A.eikonal3d_grad(gu, u, u0, f, h, m, n, l)[1], gu
+
+        def cpu(gu):
+            u, _, _ = O.eik3d_forward(u0, f, h, 1e-6)
+            return u, O.eik3d_backward(gu, u, u0, f, h)[1]
+        desc = ("C2: 3D 64x64x32, h=1 km, layered 4-8 km/s x (1+-5%) checkerboard, 1 interior "
+                "source, 50 surface receivers, +2%-noise picks, tol 1e-6, 20-iteration cap")
+    for _ in range(args.warmup):
+        gpu()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u, gf, gu = gpu()
+    gpu_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    reps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ur, rf = cpu(gu)
+    cpu_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    line = {
+        "metric": "plain FP64 forward + adjoint, time per event (host buffers)",
+        "value": gpu_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": desc},
+        "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": 1, "kind": "port",
+                         "sample": f"the same event, {reps} repetitions (oracle port, FP64)"},
+        "parity": {"forward_bit_identical": bool(np.array_equal(u, ur)),
+                   "grad_max_rel": float(np.max(np.abs(gf - rf)) / np.max(np.abs(rf)))},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_inversion(args):
     """10 L-BFGS iterations of the inversion driver in FP32 and in FP64 on the
     C3 grid, stations as sources (scripts/inversion.jl): time per iteration
@@ -472,8 +680,10 @@ def main():
     ap.add_argument("--groups", type=int, default=0, help="solves per CTA (0 = as many as fit)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: time candidate launch shapes on the workload first (untimed setup)")
-    ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5", "inversion"],
-                    help="c3 (default): the headline; c4, c5: secondary lines for the larger "
+    ap.add_argument("--workload", default="c3",
+                    choices=["c1", "c2", "c3", "c4", "c5", "inversion"],
+                    help="c3 (default): the headline; c1, c2: the plain FP64 single-event "
+                         "configurations; c4, c5: secondary lines for the larger "
                          "configurations")
     ap.add_argument("--wake-tol", type=float, default=1e-6,
                     help="forward: a brick that moved by at most this (s) wakes no neighbour "
@@ -483,7 +693,10 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,
-                    help="events timed for the cpu_baseline (0 skips it)")
+                    help="events timed for the cpu_baseline and compared for error_vs_fp64 "
+                         "(0 skips both)")
+    ap.add_argument("--fp64-batched", type=int, default=1,
+                    help="1: time the same batched plan in FP64 as a yardstick (untimed leg)")
     args = ap.parse_args()
     N_EVENTS = args.events
     rank = int(os.environ.get("RANK", "0"))
@@ -494,6 +707,10 @@ def main():
     if args.workload == "inversion":
         if rank == 0:
             run_inversion(args)
+        return
+    if args.workload in ("c1", "c2"):
+        if rank == 0:
+            run_single(args)
         return
     if args.workload != "c3":
         if rank == 0:

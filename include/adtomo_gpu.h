@@ -189,6 +189,10 @@ typedef struct adt_batch_opts {
                            |new - old| / |new| in a sweep is at most adj_wake_tol wakes
                            no neighbour and does not extend the solve; 0 (default) =
                            exact (iterate until nothing changes).  Ignored in FP64. */
+  int32_t adj_order_filter; /* 1 (default): the adjoint sweeps a brick only in the
+                           orderings that follow the directions its adjoint values
+                           flow in (exact: same fixed point, same bits); 0: every
+                           ordering */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;

@@ -7,9 +7,11 @@ Follows tests/Eikonal/eikoloc.py: _interp (:119-145, bilinear with the cell
 index clamped to the table), traveltime (:148-156, r = horizontal distance,
 z = |z_event| - z_station), and the closure of invert (:169-204: position
 clamped to the bounds, mean weighted Huber loss per phase, optional
-double-difference term weighted by gamma).  Parity is unpinned: the
-reference needs torch and pandas, and its data are not shipped, so the
-restatement is checked by finite differences and against SciPy.
+double-difference term weighted by gamma).  Pinned: tests/test_oracle.py
+checks it against tests/golden/loc_eikoloc.npz, the loss and autograd
+gradient of the script's own _interp, traveltime and invert closure on seeded
+tables and picks (generated by tests/golden/make_location_golden.py, which
+executes those functions from the script's source).
 """
 from __future__ import annotations
 

@@ -22,7 +22,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "g[23]d_*.npz")))
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -284,6 +284,62 @@ def test_batch_fp32_accuracy_against_fp64():
     B.close()
 
 
+def _fp32_vs_fp64_full_grid(fields, stations, slow, slow_obs, sf, src):
+    """FP32 plan with the bench's wake tolerances against the reference's FP64
+    op (the oracle: tol 1e-6, 20 iterations, exact causal adjoint) on the same
+    picks: FP64 travel times on the perturbed model (the library's FP64 plan
+    with the reference stopping rule, bit-exact to the oracle)."""
+    n_obs = sum(len(stations[fi]) for fi in sf)
+    w = np.ones(n_obs)
+    P = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True)
+    _, t_obs, _, _ = P.run(slow_obs, np.full(n_obs, 1.0), w)
+    P.close()
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, wake_tol=1e-6,
+                  adj_wake_tol=1e-5)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    B.close()
+    assert all(s.converged and s.adj_converged for s in st)
+    mo, tpo, go, _ = O.batch_misfit_grad([(s_, f_[3]) for s_, f_ in zip(slow, fields)], stations,
+                                         sf, src, t_obs, w, tol=1e-6, max_iter=20,
+                                         nthreads=os.cpu_count() or 1)
+    # tolerances: travel times 1e-4 relative (max over picks), gradient 1e-3
+    # relative (L2, each field), misfit 1e-3 relative
+    assert np.max(np.abs(tp - tpo) / tpo) <= 1e-4
+    assert abs(mis - mo) <= 1e-3 * mo
+    for g, r in zip(grads, go):
+        assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
+
+
+def test_batch_fp32_c3_full_grid_against_fp64():
+    """The headline configuration's grid at full size: 128x128x64, h = 0.5 km,
+    layered 4-8 km/s x (1 +- 5%) 8-cell checkerboard, 100 surface stations,
+    8 events uniform in the volume, picks from a +2%-noise model."""
+    rng = np.random.default_rng(0)
+    m, n, l, h = 128, 128, 64, 0.5
+    f = synth.layered_checkerboard(m, n, l, block=8)
+    sta = synth.surface_stations(m, n, 100, rng)
+    src = synth.volume_sources(m, n, l, 8, rng)
+    f_obs = f / (1.0 + 0.02 * rng.standard_normal(f.shape))
+    _fp32_vs_fp64_full_grid([(m, n, l, h)], [sta], [f], [f_obs], np.zeros(8, np.int32), src)
+
+
+def test_batch_fp32_c4_largest_grid_p_and_s_against_fp64():
+    """The uneven P/S configuration's largest grid at full size: 160x160x80,
+    h = 0.5 km, Vp layered 4-8 km/s x (1 +- 5%) smooth, Vs = Vp / 1.73, 150
+    surface stations, 2 events with a P and an S solve each."""
+    rng = np.random.default_rng(4)
+    m, n, l, h = 160, 160, 80, 0.5
+    vp = synth.layered_smooth(m, n, l, rng)
+    sta = synth.surface_stations(m, n, 150, rng)
+    ev = synth.volume_sources(m, n, l, 2, rng)
+    fields = [(m, n, l, h), (m, n, l, h)]
+    slow = [1.0 / vp, 1.73 / vp]
+    slow_obs = [s_ * 1.02 for s_ in slow]
+    sf = np.array([0, 1, 0, 1], np.int32)
+    src = np.repeat(ev, 2, axis=0)
+    _fp32_vs_fp64_full_grid(fields, [sta, sta], slow, slow_obs, sf, src)
+
+
 def test_batch_fp32_wake_tolerances_against_fp64():
     """Bricks that moved by at most wake_tol (forward, seconds) or adj_wake_tol
     (adjoint, relative) wake no neighbours: results stay within the FP32
@@ -315,6 +371,31 @@ def test_batch_fp32_wake_tolerances_against_fp64():
         A.Batch3D(fields, stations, sf, src, wake_tol=-1.0)
     with pytest.raises(A.AdtError):
         A.Batch3D(fields, stations, sf, src, adj_wake_tol=float("nan"))
+
+
+def test_batch_adjoint_order_filter_is_exact():
+    """Sweeping each adjoint brick only in the orderings that follow its flow
+    (adt_batch_opts.adj_order_filter, the default) reaches the same unique
+    fixed point of the triangular adjoint system: with exact skipping the
+    predicted times, misfit and gradient are bit-identical with and without
+    the filter, in FP32 and FP64, while fewer bricks are swept."""
+    rng = np.random.default_rng(21)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(40, 36, 24, 0.5), (24, 24, 48, 0.5)], 8, 12)
+    for prec in (A.ADT_F32, A.ADT_F64):
+        out = []
+        for filt in (True, False):
+            B = A.Batch3D(fields, stations, sf, src, precision=prec, tol=1e-7,
+                          adj_order_filter=filt)
+            mis, tp, grads, st = B.run(slow, t_obs, w)
+            out.append((mis, tp, grads, B.stats().adj_bricks, st))
+            B.close()
+        (m1, tp1, g1, b1, st1), (m0, tp0, g0, b0, st0) = out
+        assert m1 == m0 and np.array_equal(tp1, tp0), prec
+        for a, b in zip(g1, g0):
+            assert np.array_equal(a, b), prec
+        assert all(s.adj_converged for s in st1) and all(s.adj_converged for s in st0)
+        assert b1 < b0, (prec, b1, b0)
 
 
 def test_batch_run_into_caller_buffers():

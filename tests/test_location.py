@@ -61,6 +61,30 @@ def test_loss_and_gradient_match_numpy(gamma):
         assert np.allclose(grad[:, a], fd, rtol=1e-5, atol=1e-7), a
 
 
+def test_loss_and_gradient_match_the_reference_script(golden_dir):
+    """adt_locate_loss_grad against the loss and autograd gradient of the
+    reference's own location code (tests/Eikonal/eikoloc.py: _interp,
+    traveltime and the closure of invert, executed by
+    tests/golden/make_location_golden.py): loss to 1e-12 relative, gradient to
+    1e-9 relative, with and without the double-difference term."""
+    import os
+    d = np.load(os.path.join(golden_dir, "loc_eikoloc.npz"))
+    offs = d["offs"]
+    for gamma in np.unique(d["gamma"]):
+        ev = np.flatnonzero(d["gamma"] == gamma)
+        sub_offs, idx = [0], []
+        for e in ev:
+            idx.extend(range(offs[e], offs[e + 1]))
+            sub_offs.append(len(idx))
+        picks = {"offs": np.array(sub_offs), "sta": d["sta"][idx], "t": d["t"][idx],
+                 "phase": d["phase"][idx].astype(np.int32), "w": d["w"][idx]}
+        loc = Lc.Locator(d["tp"], d["ts"], float(d["r0"]), float(d["z0"]), float(d["h"]),
+                         d["bounds"], gamma=float(gamma))
+        loss, grad = loc.loss_grad(d["params"][ev], picks)
+        assert np.allclose(loss, d["loss"][ev], rtol=1e-12, atol=0), gamma
+        assert np.allclose(grad, d["grad"][ev], rtol=1e-9, atol=1e-12), gamma
+
+
 def test_tables_match_the_2d_solver():
     tp, ts, r0, z0 = Lc.traveltime_tables(ZZ, VP, 1.73, (0.0, 30.0), (0.0, 20.0), 1.0)
     assert tp.shape == ts.shape == (33, 23) and (r0, z0) == (-3.0, -3.0)

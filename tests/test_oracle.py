@@ -16,7 +16,7 @@ import pytest
 from adtomo_gb300 import synth
 from oracle import oracle as O
 
-GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "g[23]d_*.npz")))
 
 
 @pytest.mark.parametrize("path", GOLD, ids=[os.path.basename(p)[:-4] for p in GOLD])
@@ -205,3 +205,28 @@ def test_src_u0_rules_follow_the_reference_callers(src1):
                           _julia_u0(f, h, *src1, "gene_obs"))
     assert np.array_equal(O.src_u0(v0, h, src0, mode="inversion"),
                           _julia_u0(v0, h, *src1, "inversion"))
+
+
+def test_location_oracle_matches_the_reference_script(golden_dir):
+    """The NumPy restatement of the location objective against the loss and
+    autograd gradient of tests/Eikonal/eikoloc.py's own _interp, traveltime
+    and invert closure (fixture from tests/golden/make_location_golden.py):
+    loss to 1e-12 relative, central differences of the loss to the gradient
+    to 1e-6."""
+    from oracle import location_oracle as LO
+    d = np.load(os.path.join(golden_dir, "loc_eikoloc.npz"))
+    offs, b = d["offs"], d["bounds"]
+    args = (d["tp"], d["ts"], float(d["r0"]), float(d["z0"]), float(d["h"]), b)
+    for c in range(len(d["params"])):
+        sl = slice(offs[c], offs[c + 1])
+        pick = (d["sta"][sl], d["t"][sl], d["phase"][sl], d["w"][sl])
+
+        def f(p):
+            return LO.event_loss(p, *pick, *args, gamma=float(d["gamma"][c]))
+        p0 = d["params"][c]
+        assert abs(f(p0) - d["loss"][c]) <= 1e-12 * abs(d["loss"][c]), c
+        for a in range(4):
+            e = np.zeros(4)
+            e[a] = 1e-6
+            fd = (f(p0 + e) - f(p0 - e)) / 2e-6
+            assert abs(fd - d["grad"][c][a]) <= 1e-6 * max(1.0, abs(d["grad"][c][a])), (c, a)
