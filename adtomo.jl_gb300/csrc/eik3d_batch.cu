@@ -192,6 +192,7 @@ void batch_opts_default(adt_batch_opts* o) {
   o->wake_tol = 0.0;
   o->adj_wake_tol = 0.0;
   o->adj_order_filter = 1;
+  o->fwd_order_filter = 0;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -587,6 +588,7 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.meta_smem = P.meta_smem;
   A.max_nb = P.max_nb;
   A.adj_order_filter = P.opts.adj_order_filter ? 1 : 0;
+  A.fwd_order_filter = (!P.f64 && P.opts.fwd_order_filter) ? 1 : 0;
   return A;
 }
 

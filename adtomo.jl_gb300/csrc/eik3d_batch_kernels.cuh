@@ -84,6 +84,8 @@ struct BatchArgs {
   int meta_smem;            // 1: brick meta of the running solve in shared memory
   int max_nb;               // bricks of the largest field (shared-memory meta size)
   int adj_order_filter;     // 1: adjoint sweeps a brick only in the orderings its flow allows
+  int fwd_order_filter;     // 1: FP32 forward sweeps a brick only in the orderings its
+                            //    learned upwind directions allow
 };
 
 // Per-group scalars at the start of dynamic shared memory.
@@ -100,9 +102,10 @@ __device__ __forceinline__ void group_sync(int grp, int nthreads) {
 // Brick metadata of one solve: arrays of one int per brick.  Both sweeps keep
 // mod and proc (timestamps of the last change and of the last sweep); the
 // adjoint adds flow (the directions in which adjoint values enter the
-// brick's cells, which orderings it is swept in).  The global meta buffer
+// brick's cells, which orderings it is swept in) and the FP32 forward its
+// learned upwind directions (fmask, run_ordering).  The global meta buffer
 // holds META_ARRAYS_MAX arrays per solve.
-constexpr int META_ARRAYS_FWD = 2;
+constexpr int META_ARRAYS_FWD = 3;
 constexpr int META_ARRAYS_ADJ = 3;
 constexpr int META_ARRAYS_MAX = 3;
 
@@ -280,14 +283,26 @@ __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx&
 // face neighbours that feed it make it dirty (brick_dirty).  flow is written
 // before the sweeps and not during them, so every warp still reads the same
 // mask.
+//
+// fmask (FP32 forward only, else null): per brick, the upwind directions its
+// changing sweeps have seen, learned during the solve (FWD_FLOW_KNOWN set
+// once one has), with the level time of the last write in the bits above 8.
+// A dirty brick with a known mask is swept only in the orderings that follow
+// it.  The sweeper writes the entry while other warps may still be testing
+// the brick in the same level; an entry written at the current level time
+// reads as allowed, which is what the sweeper found before it swept, so all
+// warps still agree.  body(p, fbits) returns the sweep's upwind bits
+// (absolute, as the adjoint's flow bits) in fbits.
+constexpr int FWD_FLOW_KNOWN = 0x80;
+
 template <int BK, class Body>
 __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, const uint32_t* bricks,
                                              const int* lstart, int* mod, int* proc,
-                                             const int* flow, int ts0, int si, int sj, int sk,
-                                             unsigned long long& cnt_upd,
+                                             const int* flow, int* fmask, int ts0, int si, int sj,
+                                             int sk, unsigned long long& cnt_upd,
                                              unsigned long long& cnt_brk, Body&& body) {
   const int lane = c.lane;
-  const int forbid = flow ? adjoint_flow_forbidden(si, sj, sk) : 0;
+  const int forbid = (flow || fmask) ? adjoint_flow_forbidden(si, sj, sk) : 0;
   for (int d = 0; d < g.nlev; ++d) {
     const int t = ts0 + d;
     const int q0 = lstart[d], q1 = lstart[d + 1];
@@ -307,6 +322,10 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
         if (flow) {
           const int fl = ((const volatile int*)flow)[b];
           dv = adjoint_flow_allowed(fl, forbid) && brick_dirty(mod, proc, g, b, bx, by, bz, t, fl);
+        } else if (fmask) {
+          const int e = ((const volatile int*)fmask)[b];
+          dv = brick_dirty(mod, proc, g, b, bx, by, bz, t) &&
+               (!(e & FWD_FLOW_KNOWN) || (e >> 8) == t || adjoint_flow_allowed(e & 63, forbid));
         } else {
           dv = brick_dirty(mod, proc, g, b, bx, by, bz, t);
         }
@@ -318,12 +337,18 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
         const uint32_t pk = __shfl_sync(0xffffffffu, packed, bit);
         if (slot == c.gw) {
           const BrickPos p = brick_pos<BK>(g, pk, si, sj, sk);
-          const bool ch = body(p);
+          uint32_t fbits = 0;
+          const bool ch = body(p, fbits);
           __syncwarp();
           if (lane == 0) {
             const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
             proc[b] = t;
             if (ch) mod[b] = t;
+            if (fmask && fbits) {
+              const int old = fmask[b];
+              fmask[b] = (t << 8) | FWD_FLOW_KNOWN | ((old & FWD_FLOW_KNOWN) ? (old & 63) : 0) |
+                         (int)fbits;
+            }
             cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
             cnt_brk += 1;
           }
@@ -337,28 +362,30 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
 
 // Select the sweep instantiation for the ordering's directions and the
 // near-source flag.
-template <int BK, int SI, int SJ, int SKD>
+template <int BK, int SI, int SJ, int SKD, bool FLOW>
 __device__ __forceinline__ bool fwd_f32_dir(float* S, const float* F, const BrickPos& p, bool nr,
                                             float h, double hd, const NearBox& box, int lane,
-                                            float& md) {
-  return nr ? sweep_brick_fwd_f32<BK, SI, SJ, SKD, true>(S, F, p, h, hd, box, lane, md)
-            : sweep_brick_fwd_f32<BK, SI, SJ, SKD, false>(S, F, p, h, hd, box, lane, md);
+                                            float& md, uint32_t& fbits) {
+  return nr ? sweep_brick_fwd_f32<BK, SI, SJ, SKD, true, FLOW>(S, F, p, h, hd, box, lane, md,
+                                                               fbits)
+            : sweep_brick_fwd_f32<BK, SI, SJ, SKD, false, FLOW>(S, F, p, h, hd, box, lane, md,
+                                                                fbits);
 }
 
-template <int BK>
+template <int BK, bool FLOW>
 __device__ __forceinline__ bool dispatch_fwd_f32(float* S, const float* F, const BrickPos& p,
                                                  int si, int sj, int sk, bool nr, float h,
                                                  double hd, const NearBox& box, int lane,
-                                                 float& md) {
+                                                 float& md, uint32_t& fb) {
   switch ((si < 0) | ((sj < 0) << 1) | ((sk < 0) << 2)) {
-    case 0: return fwd_f32_dir<BK, 1, 1, 1>(S, F, p, nr, h, hd, box, lane, md);
-    case 1: return fwd_f32_dir<BK, -1, 1, 1>(S, F, p, nr, h, hd, box, lane, md);
-    case 2: return fwd_f32_dir<BK, 1, -1, 1>(S, F, p, nr, h, hd, box, lane, md);
-    case 3: return fwd_f32_dir<BK, -1, -1, 1>(S, F, p, nr, h, hd, box, lane, md);
-    case 4: return fwd_f32_dir<BK, 1, 1, -1>(S, F, p, nr, h, hd, box, lane, md);
-    case 5: return fwd_f32_dir<BK, -1, 1, -1>(S, F, p, nr, h, hd, box, lane, md);
-    case 6: return fwd_f32_dir<BK, 1, -1, -1>(S, F, p, nr, h, hd, box, lane, md);
-    default: return fwd_f32_dir<BK, -1, -1, -1>(S, F, p, nr, h, hd, box, lane, md);
+    case 0: return fwd_f32_dir<BK, 1, 1, 1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    case 1: return fwd_f32_dir<BK, -1, 1, 1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    case 2: return fwd_f32_dir<BK, 1, -1, 1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    case 3: return fwd_f32_dir<BK, -1, -1, 1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    case 4: return fwd_f32_dir<BK, 1, 1, -1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    case 5: return fwd_f32_dir<BK, -1, 1, -1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    case 6: return fwd_f32_dir<BK, 1, -1, -1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
+    default: return fwd_f32_dir<BK, -1, -1, -1, FLOW>(S, F, p, nr, h, hd, box, lane, md, fb);
   }
 }
 
@@ -385,6 +412,8 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
     const int nb = g.nbx * g.nby * g.nbz;
     int* mod = c.smeta ? c.smeta : A.meta + sd.meta_off;
     int* proc = mod + (c.smeta ? A.max_nb : nb);
+    int* fmask = (MODE == MODE_STABLE && A.fwd_order_filter) ? proc + (c.smeta ? A.max_nb : nb)
+                                                               : nullptr;
     // u = u0 (column-wise: lanes along k)
     for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
@@ -406,6 +435,7 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
                        near(sd.zf, sd.zc, bz, BK);
       mod[b] = src ? -1 : -2;
       proc[b] = -1;
+      if (fmask) fmask[b] = 0;
     }
     NearBox box;
     box.i0 = max(0, sd.xf - A.near_r);
@@ -431,8 +461,9 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
         int si, sj, sk;
         ordering3(o, si, sj, sk);
         const int CS = tile_col_stride(BK, sj == sk);
-        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, nullptr, (it * 8 + o) * g.nlev,
-                         si, sj, sk, cnt_upd, cnt_brk, [&](const BrickPos& p) -> bool {
+        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, nullptr, fmask,
+                         (it * 8 + o) * g.nlev, si, sj, sk, cnt_upd, cnt_brk,
+                         [&](const BrickPos& p, uint32_t& fbits) -> bool {
           bool ch;
           if constexpr (MODE == MODE_STABLE && sizeof(T) == 4) {
             if (vec) {
@@ -442,7 +473,10 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
               __syncwarp();
               const bool nr = use_near && box.hits(p);
               float mbb = 0.0f;  // this brick's largest decrease (per lane)
-              ch = dispatch_fwd_f32<BK>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box, lane, mbb);
+              ch = fmask ? dispatch_fwd_f32<BK, true>(S, F, p, si, sj, sk, nr, (float)h, fd.h, box,
+                                                      lane, mbb, fbits)
+                         : dispatch_fwd_f32<BK, false>(S, F, p, si, sj, sk, nr, (float)h, fd.h,
+                                                       box, lane, mbb, fbits);
               md = fmaxf(md, mbb);
               if (ch) store_interior_f32_vec<BK>(S, u, g, p, CS, lane);
               // the brick's own cells keep every decrease; only a brick that moved by
@@ -899,8 +933,8 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         ordering3(o, si, sj, sk);
         const int CS = tile_col_stride(BK, sj == sk);
         run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, A.adj_order_filter ? flow : nullptr,
-                         (it * 8 + o) * g.nlev, si, sj, sk, cnt_upd, cnt_brk,
-                         [&](const BrickPos& p) -> bool {
+                         nullptr, (it * 8 + o) * g.nlev, si, sj, sk, cnt_upd, cnt_brk,
+                         [&](const BrickPos& p, uint32_t&) -> bool {
           bool ch;
           if constexpr (sizeof(T) == 4) {
             if (vec) {

@@ -475,10 +475,16 @@ __device__ __forceinline__ void sts_if(bool p, uint32_t a, float v) {
 // the carried old value at kk = -1 is the halo cell, so the z-upstream value
 // entering the window is right without a special case.  SI, SJ, SKD: sweep
 // directions; NEAR: cells in the source box update in FP64.
-template <int BK, int SI, int SJ, int SKD, bool NEAR>
+//
+// FLOW: also collect the upwind directions of the written cells into fbits
+// (bit 0: some cell's active x neighbour is its x- one, so values travel
+// along +x; bit 1: along -x; bits 2-3 y, 4-5 z).  An axis is active when the
+// new value exceeds the smaller neighbour along it; that neighbour is the
+// upwind one (ties: the sweep-upstream one).
+template <int BK, int SI, int SJ, int SKD, bool NEAR, bool FLOW = false>
 __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, const BrickPos& p,
                                                     float h, double hd, const NearBox& nb,
-                                                    int lane, float& maxdec) {
+                                                    int lane, float& maxdec, uint32_t& fbits) {
   constexpr int RS = tile_row_stride(BK);
   constexpr int IRS = itile_row_stride(BK);
   constexpr int CS = tile_col_stride(BK, SJ == SKD);
@@ -500,6 +506,7 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
   float dn = lds<DZ>(a), xd = lds<XD>(a), yd = lds<YD>(a);
   float fc = lds<0>(fa);
   float mb = 0.0f;
+  uint32_t fl = 0;  // sweep-relative upwind bits: 1/2 x up-/downstream, 4/8 y, 16/32 z
   const int nsteps = p.nk + SKEW;
 #pragma unroll 4
   for (int tau = 0; tau < nsteps; ++tau) {
@@ -520,6 +527,12 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
     const bool wr = act && (un < uo);
     sts_if(wr, a, un);
     mb = fmaxf(mb, act ? uo - un : 0.0f);
+    if constexpr (FLOW) {
+      const uint32_t bx = (un > ax) ? ((xu <= xd) ? 1u : 2u) : 0u;
+      const uint32_t by = (un > ay) ? ((yu <= yd) ? 4u : 8u) : 0u;
+      const uint32_t bz = (un > az) ? ((prev <= dn) ? 16u : 32u) : 0u;
+      fl |= wr ? (bx | by | bz) : 0u;
+    }
     prev = wr ? un : uo;
     uo = dn;
     dn = n_dn;
@@ -531,6 +544,15 @@ __device__ __forceinline__ bool sweep_brick_fwd_f32(float* S, const float* F, co
     __syncwarp();
   }
   maxdec = fmaxf(maxdec, mb);
+  if constexpr (FLOW) {
+    // to absolute directions: the sweep-upstream side is the minus side of a
+    // positive sweep direction
+    uint32_t r = __reduce_or_sync(0xffffffffu, fl);
+    if (SI < 0) r = (r & ~3u) | ((r & 1u) << 1) | ((r >> 1) & 1u);
+    if (SJ < 0) r = (r & ~12u) | ((r & 4u) << 1) | ((r >> 1) & 4u);
+    if (SKD < 0) r = (r & ~48u) | ((r & 16u) << 1) | ((r >> 1) & 16u);
+    fbits = r;
+  }
   return __any_sync(0xffffffffu, mb > 0.0f);
 }
 

@@ -284,7 +284,7 @@ def run_ours(args, rank, world):
     t_obs = gpu_picks(A)
     B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
                   warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
-                  adj_wake_tol=args.adj_wake_tol)
+                  adj_wake_tol=args.adj_wake_tol, fwd_order_filter=bool(args.fwd_order_filter))
     B.upload([f], t_obs, w)
     if args.autotune and not (args.warps or args.groups):
         B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
@@ -380,7 +380,8 @@ def run_ours(args, rank, world):
         # events, picks and options as the headline plan (untimed)
         k = cpu_sample
         E = A.Batch3D([(M, N, L, H)], [sta], np.zeros(k, np.int32), src[:k], precision=A.ADT_F32,
-                      tol=1e-6, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol)
+                      tol=1e-6, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
+                      fwd_order_filter=bool(args.fwd_order_filter))
         mis_k, tp_k, (g_k,), _ = E.run([f], t_obs[:k * N_STA], w[:k * N_STA])
         E.close()
         mo, tpo, go = cpu_out
@@ -424,6 +425,7 @@ def run_ours(args, rank, world):
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
                    "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
+                   "fwd_order_filter": args.fwd_order_filter,
                    "picks": "FP64 travel times on the +2%-noise model (reference stopping rule)",
                    "vs_exact_skipping": vs_exact, "error_vs_fp64": err64},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
@@ -666,6 +668,85 @@ def run_inversion(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c5_inversion(args):
+    """The inversion-scale configuration as specified: 10 L-BFGS iterations of
+    the inversion driver (scripts/inversion.jl around src/mpi_optimize.jl) on
+    256x256x128, h = 0.25 km, 2000 events uniform in the volume and 300
+    surface stations on the layered+checkerboard model, FP32, forward fields
+    recomputed per 128-event chunk.  By reciprocity the events are the sources
+    (2000 solves in chunks of 128) and the stations the receivers.  Picks come
+    from the true model through the same plan (gene_obs.jl's near-source rule);
+    the inversion starts from the true model's depth average and builds u0
+    from it (inversion.jl's rule).  Reported: seconds per L-BFGS iteration,
+    the loss history and the model error against the true model; then the
+    FP32 run against the FP64 run on a stated reduction (the first
+    --c5-fp64-events events, --c5-fp64-iters iterations): relative difference
+    of the model updates."""
+    import torch  # noqa: F401  (CUDA context through the library)
+    import adtomo_gb300 as A
+    from adtomo_gb300 import synth
+    from adtomo_gb300.inversion import TravelTimeInversion
+    rng = np.random.default_rng(SEED)
+    m, n, l, h = 256, 256, 128, 0.25
+    n_eve, n_sta, chunk = 2000, 300, 128
+    f_true = synth.layered_checkerboard(m, n, l, block=8)
+    v_true = 1.0 / f_true
+    vel0 = np.broadcast_to(v_true.mean(axis=(0, 1), keepdims=True), v_true.shape).copy()
+    sta = synth.surface_stations(m, n, n_sta, rng)
+    eve = synth.volume_sources(m, n, l, n_eve, rng)
+    opts = dict(tol=1e-6, max_iter=200, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
+                chunk=chunk)
+    t0 = time.perf_counter()
+    P = A.Batch3D([(m, n, l, h)], [sta], np.zeros(n_eve, np.int32), eve, precision=A.ADT_F32,
+                  **opts)
+    _, tp, _, _ = P.run([f_true], np.full(n_eve * n_sta, 1.0), np.ones(n_eve * n_sta))
+    P.close()
+    picks_s = time.perf_counter() - t0
+    uobs = tp.reshape(n_eve, n_sta)
+    qua = np.ones_like(uobs)
+
+    def invert(k_eve, iters, prec):
+        inv = TravelTimeInversion((m, n, l, h), vel0, eve[:k_eve], sta, uobs[:k_eve], qua[:k_eve],
+                                  lambda_p=0.0, precision=prec, **opts)
+        t1 = time.perf_counter()
+        x, loss, hist = inv.optimize(iterations=iters)
+        dt = time.perf_counter() - t1
+        v = inv.velocity(x)
+        out = {"s": dt, "hist": hist, "evaluations": inv.evaluations, "v": v}
+        inv.close()
+        return out
+
+    full = invert(n_eve, args.steps, A.ADT_F32)
+    k64, it64 = args.c5_fp64_events, args.c5_fp64_iters
+    r32 = invert(k64, it64, A.ADT_F32) if k64 > 0 else None
+    r64 = invert(k64, it64, A.ADT_F64) if k64 > 0 else None
+    err0 = np.linalg.norm(vel0 - v_true)
+    line = {
+        "metric": "C5 L-BFGS time per iteration (s), FP32, 2000 events in 128-event chunks",
+        "value": full["s"] / max(len(full["hist"]), 1), "unit": "s/iteration", "n_gpus": 1,
+        "steps": args.steps, "higher_is_better": False, "dtype": "f32",
+        "data": "synthetic (seeded): true layered+checkerboard, start = its depth average",
+        "config": {"workload": "C5: 256x256x128, h=0.25 km, 2000 events (sources, 128-event "
+                               "chunks, forward recomputed per chunk) and 300 surface stations, "
+                               f"{args.steps} L-BFGS iterations of the inversion driver",
+                   "iterations": len(full["hist"]), "evaluations": full["evaluations"],
+                   "seconds_total": full["s"], "picks_setup_s": picks_s,
+                   "loss_history": full["hist"],
+                   "model_error_rel": float(np.linalg.norm(full["v"] - v_true) / err0),
+                   "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol},
+    }
+    if r64 is not None:
+        dv64 = np.linalg.norm(r64["v"] - vel0)
+        line["config"]["vs_fp64"] = {
+            "reduction": f"first {k64} events, {it64} L-BFGS iterations (FP64 plan with the "
+                         "same options; wake tolerances apply to FP32 only)",
+            "model_update_rel_diff": float(np.linalg.norm(r32["v"] - r64["v"]) / max(dv64, 1e-300)),
+            "f32_loss": r32["hist"], "f64_loss": r64["hist"],
+            "f32_s_per_iteration": r32["s"] / max(len(r32["hist"]), 1),
+            "f64_s_per_iteration": r64["s"] / max(len(r64["hist"]), 1)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global N_EVENTS
     ap = argparse.ArgumentParser()
@@ -681,20 +762,28 @@ def main():
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: time candidate launch shapes on the workload first (untimed setup)")
     ap.add_argument("--workload", default="c3",
-                    choices=["c1", "c2", "c3", "c4", "c5", "inversion"],
+                    choices=["c1", "c2", "c3", "c4", "c5", "c5inv", "inversion"],
                     help="c3 (default): the headline; c1, c2: the plain FP64 single-event "
                          "configurations; c4, c5: secondary lines for the larger "
-                         "configurations")
+                         "configurations; c5inv: C5's 10 L-BFGS iterations; inversion: the "
+                         "inversion driver on the C3 grid, FP32 against FP64")
     ap.add_argument("--wake-tol", type=float, default=1e-6,
                     help="forward: a brick that moved by at most this (s) wakes no neighbour "
                          "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
     ap.add_argument("--adj-wake-tol", type=float, default=1e-5,
                     help="adjoint: the same for relative changes (default 1e-5; 0 = exact)")
+    ap.add_argument("--fwd-order-filter", type=int, default=0,
+                    help="1: FP32 forward sweeps each brick only in the orderings that follow "
+                         "its learned upwind directions")
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,
                     help="events timed for the cpu_baseline and compared for error_vs_fp64 "
                          "(0 skips both)")
+    ap.add_argument("--c5-fp64-events", type=int, default=128,
+                    help="c5inv: events of the FP32-vs-FP64 comparison (0 skips it)")
+    ap.add_argument("--c5-fp64-iters", type=int, default=2,
+                    help="c5inv: L-BFGS iterations of the FP32-vs-FP64 comparison")
     ap.add_argument("--fp64-batched", type=int, default=1,
                     help="1: time the same batched plan in FP64 as a yardstick (untimed leg)")
     args = ap.parse_args()
@@ -707,6 +796,10 @@ def main():
     if args.workload == "inversion":
         if rank == 0:
             run_inversion(args)
+        return
+    if args.workload == "c5inv":
+        if rank == 0:
+            run_c5_inversion(args)
         return
     if args.workload in ("c1", "c2"):
         if rank == 0:

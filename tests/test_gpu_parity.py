@@ -398,6 +398,35 @@ def test_batch_adjoint_order_filter_is_exact():
         assert b1 < b0, (prec, b1, b0)
 
 
+def test_batch_fp32_forward_order_filter_against_fp64():
+    """FP32 forward sweeping each brick only in the orderings that follow the
+    upwind directions its sweeps have seen (adt_batch_opts.fwd_order_filter):
+    the same fixed point along another iteration path, so results stay within
+    the FP32 tolerances of the converged FP64 oracle (travel times 1e-4
+    relative, gradient 1e-3 relative L2), alone and with the wake tolerances,
+    and do not depend on the launch shape."""
+    rng = np.random.default_rng(8)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(40, 36, 24, 0.5), (24, 24, 48, 0.5)], 8, 12)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    ok = tpo > 0
+    first = None
+    for kw in ({}, {"warps": 3, "groups": 2}, {"wake_tol": 1e-6, "adj_wake_tol": 1e-5}):
+        B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7,
+                      fwd_order_filter=True, **kw)
+        mis, tp, grads, st = B.run(slow, t_obs, w)
+        B.close()
+        assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4, kw
+        assert abs(mis - mo) <= 1e-3 * mo, kw
+        for g, r in zip(grads, go):
+            assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r), kw
+        assert all(s.converged and s.adj_converged for s in st), kw
+        if first is None:
+            first = (tp, grads[0])
+        elif "warps" in kw:
+            assert np.array_equal(tp, first[0]) and np.array_equal(grads[0], first[1])
+
+
 def test_batch_run_into_caller_buffers():
     rng = np.random.default_rng(12)
     fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 5, 6)
@@ -426,7 +455,13 @@ def test_batch_chunking_and_graph_do_not_change_results():
         assert out[0] == r[0], kw
         assert np.array_equal(out[1], r[1]), kw
         assert np.array_equal(out[2][0], r[2][0]), kw
-        assert [(x.iters, x.adj_iters) for x in out[3]] == [(x.iters, x.adj_iters) for x in r[3]], kw
+        # the adjoint's ordering filter is per brick, so its iteration path (not its
+        # fixed point) depends on the brick depth
+        if "bk" in kw:
+            assert [x.iters for x in out[3]] == [x.iters for x in r[3]], kw
+        else:
+            assert ([(x.iters, x.adj_iters) for x in out[3]] ==
+                    [(x.iters, x.adj_iters) for x in r[3]]), kw
         # a second evaluation of the same plan reproduces the first
         out2 = B.run(slow, t_obs, w)
         assert np.array_equal(out2[2][0], out[2][0]), kw
