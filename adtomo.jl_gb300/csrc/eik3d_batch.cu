@@ -192,7 +192,7 @@ void batch_opts_default(adt_batch_opts* o) {
   o->wake_tol = 0.0;
   o->adj_wake_tol = 0.0;
   o->adj_order_filter = 1;
-  o->fwd_order_filter = 0;
+  o->fwd_order_filter = 1;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);

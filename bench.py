@@ -772,9 +772,9 @@ def main():
                          "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
     ap.add_argument("--adj-wake-tol", type=float, default=1e-5,
                     help="adjoint: the same for relative changes (default 1e-5; 0 = exact)")
-    ap.add_argument("--fwd-order-filter", type=int, default=0,
-                    help="1: FP32 forward sweeps each brick only in the orderings that follow "
-                         "its learned upwind directions")
+    ap.add_argument("--fwd-order-filter", type=int, default=1,
+                    help="1 (library default): FP32 forward sweeps each brick only in the "
+                         "orderings that follow its learned upwind directions; 0: all")
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,

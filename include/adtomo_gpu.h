@@ -193,10 +193,11 @@ typedef struct adt_batch_opts {
                            orderings that follow the directions its adjoint values
                            flow in (exact: same fixed point, same bits); 0: every
                            ordering */
-  int32_t fwd_order_filter; /* FP32 forward, 1: a brick is swept only in the orderings
-                           that follow the upwind directions its earlier sweeps saw
-                           (same fixed point, another iteration path); 0 (default):
-                           every ordering.  Ignored in FP64. */
+  int32_t fwd_order_filter; /* FP32 forward, 1 (default): a brick is swept only in the
+                           orderings that follow the upwind directions its earlier
+                           sweeps saw (same fixed point, another iteration path);
+                           0: every ordering.  Ignored in FP64, which keeps the
+                           reference's iteration path. */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;

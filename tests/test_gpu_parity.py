@@ -444,22 +444,35 @@ def test_batch_run_into_caller_buffers():
 
 
 def test_batch_chunking_and_graph_do_not_change_results():
+    """Chunking, graph replay and launch shapes change only the schedule: the
+    same bits and iteration counts.  The brick depth changes the bricks the
+    ordering filters work on: without the forward filter (the adjoint's is
+    exact) the results are still the same bits; with it (the FP32 default) the
+    forward stops at its tolerance after another iteration path, within 1e-6
+    relative of the same result."""
     rng = np.random.default_rng(9)
     fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(18, 14, 20, 0.5)], 7, 6)
     ref = A.Batch3D(fields, stations, sf, src, use_graph=False)
     r = ref.run(slow, t_obs, w)
+    ref_x = A.Batch3D(fields, stations, sf, src, use_graph=False, fwd_order_filter=False)
+    rx = ref_x.run(slow, t_obs, w)
     for kw in ({"chunk": 3}, {"chunk": 1, "use_graph": True}, {"bk": 64}, {"bk": 16}, {"warps": 3},
                {"warps": 1, "groups": 1}, {"warps": 2, "groups": 5}):
         B = A.Batch3D(fields, stations, sf, src, **kw)
         out = B.run(slow, t_obs, w)
-        assert out[0] == r[0], kw
-        assert np.array_equal(out[1], r[1]), kw
-        assert np.array_equal(out[2][0], r[2][0]), kw
-        # the adjoint's ordering filter is per brick, so its iteration path (not its
-        # fixed point) depends on the brick depth
         if "bk" in kw:
-            assert [x.iters for x in out[3]] == [x.iters for x in r[3]], kw
+            assert np.max(np.abs(out[1] - r[1]) / r[1]) <= 1e-6, kw
+            assert np.linalg.norm(out[2][0] - r[2][0]) <= 1e-5 * np.linalg.norm(r[2][0]), kw
+            X = A.Batch3D(fields, stations, sf, src, fwd_order_filter=False, **kw)
+            ox = X.run(slow, t_obs, w)
+            X.close()
+            assert ox[0] == rx[0] and np.array_equal(ox[1], rx[1]), kw
+            assert np.array_equal(ox[2][0], rx[2][0]), kw
+            assert [x.iters for x in ox[3]] == [x.iters for x in rx[3]], kw
         else:
+            assert out[0] == r[0], kw
+            assert np.array_equal(out[1], r[1]), kw
+            assert np.array_equal(out[2][0], r[2][0]), kw
             assert ([(x.iters, x.adj_iters) for x in out[3]] ==
                     [(x.iters, x.adj_iters) for x in r[3]]), kw
         # a second evaluation of the same plan reproduces the first
@@ -467,6 +480,7 @@ def test_batch_chunking_and_graph_do_not_change_results():
         assert np.array_equal(out2[2][0], out[2][0]), kw
         B.close()
     ref.close()
+    ref_x.close()
 
 
 def test_batch_nonconvergence_is_reported():
