@@ -93,7 +93,16 @@ struct GroupShared {
   int q;
   int changed;
   unsigned long long err;
+  int lo[2], hi[2];  // level range with pending bricks at the start of an ordering (run_ordering)
+  int lchg[3];       // a brick of level d changed in this ordering: lchg[d % 3]
 };
+
+// Empty level ranges for both orderings' slots (run_ordering), at the start
+// of a solve, before the barrier that precedes its sweeps.
+__device__ __forceinline__ void group_reset_range(GroupShared* gs) {
+  gs->lo[0] = gs->lo[1] = INT_MAX;
+  gs->hi[0] = gs->hi[1] = -1;
+}
 
 __device__ __forceinline__ void group_sync(int grp, int nthreads) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(grp + 1), "r"(nthreads) : "memory");
@@ -303,7 +312,60 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
                                              unsigned long long& cnt_brk, Body&& body) {
   const int lane = c.lane;
   const int forbid = (flow || fmask) ? adjoint_flow_forbidden(si, sj, sk) : 0;
-  for (int d = 0; d < g.nlev; ++d) {
+  // does brick b need a sweep at level time t (dirty, and allowed by the filters)?
+  auto pending = [&](int b, int bx, int by, int bz, int t) -> bool {
+    if (flow) {
+      const int fl = ((const volatile int*)flow)[b];
+      return adjoint_flow_allowed(fl, forbid) && brick_dirty(mod, proc, g, b, bx, by, bz, t, fl);
+    }
+    if (fmask) {
+      const int e = ((const volatile int*)fmask)[b];
+      return brick_dirty(mod, proc, g, b, bx, by, bz, t) &&
+             (!(e & FWD_FLOW_KNOWN) || (e >> 8) == t || adjoint_flow_allowed(e & 63, forbid));
+    }
+    return brick_dirty(mod, proc, g, b, bx, by, bz, t);
+  };
+  // Level range.  Before any sweep of this ordering, a brick needs one only if
+  // it is pending now; during the ordering a brick can become pending only
+  // when a face neighbour of the previous level changes (the next level's
+  // neighbours have not been swept yet).  So the ordering starts at the
+  // lowest pending level and stops after the highest one as soon as a level
+  // changes nothing.  Every warp scans a share of the bricks; the range and
+  // the per-level change flags live in the group's shared scalars, read only
+  // after the barriers that close their writes (lchg[d % 3] is reset during
+  // level d - 1, written during level d, read after its barrier).
+  const int par = (ts0 / g.nlev) & 1;
+  if (c.gw == 0 && lane == 0) {
+    c.gs->lchg[0] = c.gs->lchg[1] = c.gs->lchg[2] = 0;
+  }
+  {
+    int lo = INT_MAX, hi = -1;
+    const int nb = g.nbx * g.nby * g.nbz;
+    for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
+      const int bx = b / (g.nby * g.nbz), by = (b / g.nbz) % g.nby, bz = b % g.nbz;
+      if (pending(b, bx, by, bz, INT_MIN)) {
+        const int lv = (si > 0 ? bx : g.nbx - 1 - bx) + (sj > 0 ? by : g.nby - 1 - by) +
+                       (sk > 0 ? bz : g.nbz - 1 - bz);
+        lo = min(lo, lv);
+        hi = max(hi, lv);
+      }
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0 && hi >= 0) {
+      atomicMin(&c.gs->lo[par], lo);
+      atomicMax(&c.gs->hi[par], hi);
+    }
+  }
+  group_sync(c.grp, c.gthreads);
+  const int dlo = c.gs->lo[par], dhi = c.gs->hi[par];
+  if (c.gw == 0 && lane == 0) {  // the next ordering's range (nobody reads it any more)
+    c.gs->lo[par ^ 1] = INT_MAX;
+    c.gs->hi[par ^ 1] = -1;
+  }
+  for (int d = dlo; d < g.nlev; ++d) {
+    if (d > dhi && !c.gs->lchg[(d - 1) % 3]) break;
+    if (c.gw == 0 && lane == 0) c.gs->lchg[(d + 1) % 3] = 0;
     const int t = ts0 + d;
     const int q0 = lstart[d], q1 = lstart[d + 1];
     int slot = 0;
@@ -318,17 +380,7 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
         const int bx = si > 0 ? rx : g.nbx - 1 - rx;
         const int by = sj > 0 ? ry : g.nby - 1 - ry;
         const int bz = sk > 0 ? rz : g.nbz - 1 - rz;
-        const int b = (bx * g.nby + by) * g.nbz + bz;
-        if (flow) {
-          const int fl = ((const volatile int*)flow)[b];
-          dv = adjoint_flow_allowed(fl, forbid) && brick_dirty(mod, proc, g, b, bx, by, bz, t, fl);
-        } else if (fmask) {
-          const int e = ((const volatile int*)fmask)[b];
-          dv = brick_dirty(mod, proc, g, b, bx, by, bz, t) &&
-               (!(e & FWD_FLOW_KNOWN) || (e >> 8) == t || adjoint_flow_allowed(e & 63, forbid));
-        } else {
-          dv = brick_dirty(mod, proc, g, b, bx, by, bz, t);
-        }
+        dv = pending((bx * g.nby + by) * g.nbz + bz, bx, by, bz, t);
       }
       unsigned m = __ballot_sync(0xffffffffu, dv);
       while (m) {
@@ -343,7 +395,10 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
           if (lane == 0) {
             const int b = (p.bx * g.nby + p.by) * g.nbz + p.bz;
             proc[b] = t;
-            if (ch) mod[b] = t;
+            if (ch) {
+              mod[b] = t;
+              c.gs->lchg[d % 3] = 1;
+            }
             if (fmask && fbits) {
               const int old = fmask[b];
               fmask[b] = (t << 8) | FWD_FLOW_KNOWN | ((old & FWD_FLOW_KNOWN) ? (old & 63) : 0) |
@@ -437,6 +492,7 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
       proc[b] = -1;
       if (fmask) fmask[b] = 0;
     }
+    if (c.gw == 0 && lane == 0) group_reset_range(c.gs);
     NearBox box;
     box.i0 = max(0, sd.xf - A.near_r);
     box.i1 = min(g.m - 1, sd.xc + A.near_r);
@@ -871,6 +927,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
       proc[b] = -1;
       flow[b] = 0;
     }
+    if (c.gw == 0 && lane == 0) group_reset_range(c.gs);
     group_sync(c.grp, c.gthreads);
     // pass 2: users (reads only the low bits of neighbours, writes own high bits);
     // each brick's flow collects its cells' user bits
