@@ -43,7 +43,8 @@ class BatchOpts(C.Structure):
                 ("near_src_f64", C.c_int32), ("chunk", C.c_int32), ("bk", C.c_int32),
                 ("warps", C.c_int32), ("groups", C.c_int32), ("use_graph", C.c_int32),
                 ("wake_tol", C.c_double), ("adj_wake_tol", C.c_double),
-                ("adj_order_filter", C.c_int32), ("fwd_order_filter", C.c_int32)]
+                ("adj_order_filter", C.c_int32), ("fwd_order_filter", C.c_int32),
+                ("overlap_chunks", C.c_int32)]
 
 
 class BatchStats(C.Structure):

@@ -148,9 +148,19 @@ struct BatchPlan {
   // device
   DevBuf d_slow64, d_vel0, d_slowT, d_sta, d_tobs, d_w, d_tpred, d_grad, d_smis, d_mis, d_status;
   DevBuf d_levels, d_lstart, d_fields, d_solves, d_order, d_uoff;
-  DevBuf d_u, d_lam, d_code, d_meta, d_sidx, d_sval, d_nseed, d_snap, d_next, d_counters;
-  DevBuf d_gdense;  // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
-  DevBuf d_mis_scratch;  // seed merge arrays when they exceed shared memory
+  DevBuf d_nseed, d_snap, d_next, d_counters;
+  // Buffers of the solves resident at once (one chunk).  With overlapping
+  // chunks there are two sets: chunk c uses set c % 2 on stream c % 2, so the
+  // next chunk's forward runs beside this chunk's adjoint.
+  struct ChunkBufs {
+    DevBuf u, lam, code, meta, sidx, sval;
+    DevBuf gdense;       // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
+    DevBuf mis_scratch;  // seed merge arrays when they exceed shared memory
+  };
+  ChunkBufs cb[2];
+  int nsets = 1;
+  cudaStream_t stream2 = nullptr;    // second chunk stream (overlapping chunks)
+  std::vector<cudaEvent_t> ev_sync;  // [0] fork, [1 + c] gradient of chunk c added
   DevBuf d_cost, d_chunk_off, d_chunk_cnt;  // per-solve cost; chunk slices of d_order
   int64_t mis_stride = 0;
   int64_t snap_stride = 0;
@@ -172,6 +182,8 @@ struct BatchPlan {
   ~BatchPlan() {
     if (graph) cudaGraphExecDestroy(graph);
     for (auto e : ev) cudaEventDestroy(e);
+    for (auto e : ev_sync) cudaEventDestroy(e);
+    if (stream2) cudaStreamDestroy(stream2);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -193,6 +205,7 @@ void batch_opts_default(adt_batch_opts* o) {
   o->adj_wake_tol = 0.0;
   o->adj_order_filter = 1;
   o->fwd_order_filter = 1;
+  o->overlap_chunks = 0;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -423,15 +436,26 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   R_(P->d_solves, (size_t)n_solves * sizeof(SolveDev));
   R_(P->d_order, (size_t)order_total * 4);
   R_(P->d_uoff, (size_t)std::max<int64_t>(uoff_total, 1) * 8);
-  R_(P->d_u, (size_t)max_cells * es);
-  R_(P->d_lam, (size_t)max_cells * es);
-  R_(P->d_code, (size_t)max_cells * 2);
-  R_(P->d_meta, (size_t)max_bricks * 4);
-  R_(P->d_sidx, (size_t)std::max<int64_t>(max_seeds, 1) * 8);
-  R_(P->d_sval, (size_t)std::max<int64_t>(max_seeds, 1) * es);
-  if (!P->f64) {
-    R_(P->d_gdense, (size_t)max_cells * es);
-    ADT_CUDA(cudaMemset(P->d_gdense.p, 0, (size_t)max_cells * es));
+  // two buffer sets only when there is a second chunk to overlap with (the
+  // reference stopping rule's per-CTA snapshots are shared, so not there)
+  P->nsets = (o.overlap_chunks && P->chunks.size() > 1 && !o.ref_compat) ? 2 : 1;
+  for (int k = 0; k < P->nsets; ++k) {
+    BatchPlan::ChunkBufs& B = P->cb[k];
+    R_(B.u, (size_t)max_cells * es);
+    R_(B.lam, (size_t)max_cells * es);
+    R_(B.code, (size_t)max_cells * 2);
+    R_(B.meta, (size_t)max_bricks * 4);
+    R_(B.sidx, (size_t)std::max<int64_t>(max_seeds, 1) * 8);
+    R_(B.sval, (size_t)std::max<int64_t>(max_seeds, 1) * es);
+    if (!P->f64) {
+      R_(B.gdense, (size_t)max_cells * es);
+      ADT_CUDA(cudaMemset(B.gdense.p, 0, (size_t)max_cells * es));
+    }
+  }
+  if (P->nsets == 2) {
+    ADT_CUDA(cudaStreamCreateWithFlags(&P->stream2, cudaStreamNonBlocking));
+    P->ev_sync.resize(1 + P->chunks.size());
+    for (auto& e : P->ev_sync) ADT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   R_(P->d_nseed, (size_t)n_solves * 4);
   R_(P->d_next, (size_t)2 * P->chunks.size() * 4);
@@ -537,7 +561,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     P->mis_stride = (int64_t)((P->mis_smem + 255) / 256 * 256);
     int cmax = 0;
     for (auto& ch : P->chunks) cmax = std::max(cmax, ch.count);
-    R_(P->d_mis_scratch, (size_t)P->mis_stride * cmax);
+    for (int k = 0; k < P->nsets; ++k) R_(P->cb[k].mis_scratch, (size_t)P->mis_stride * cmax);
     P->mis_smem = 0;
   }
   ADT_CUDA(cudaFuncSetAttribute(P->ks.misfit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->mis_smem));
@@ -557,19 +581,21 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
 void batch_destroy(BatchPlan* P) { delete P; }
 
 template <class T>
-static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int which_counter) {
+static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int which_counter,
+                              int set) {
+  const BatchPlan::ChunkBufs& CB = P.cb[set];
   BatchArgs<T> A;
   A.fields = P.d_fields.as<FieldDev<T>>();
   A.solves = P.d_solves.as<SolveDev>();
   A.order = P.d_order.as<int>() + ch.dev_order_off;
   A.n_solves = ch.count;
-  A.u = P.d_u.as<T>();
-  A.lam = P.d_lam.as<T>();
-  A.code = P.d_code.as<uint16_t>();
-  A.meta = P.d_meta.as<int>();
-  A.seed_idx = P.d_sidx.as<int64_t>();
-  A.seed_val = P.d_sval.as<T>();
-  A.gdense = P.f64 ? nullptr : P.d_gdense.as<T>();
+  A.u = CB.u.as<T>();
+  A.lam = CB.lam.as<T>();
+  A.code = CB.code.as<uint16_t>();
+  A.meta = CB.meta.as<int>();
+  A.seed_idx = CB.sidx.as<int64_t>();
+  A.seed_val = CB.sval.as<T>();
+  A.gdense = P.f64 ? nullptr : CB.gdense.as<T>();
   A.n_seed = P.d_nseed.as<int>();
   A.snap = P.opts.ref_compat ? P.d_snap.as<T>() : nullptr;
   A.snap_stride = P.snap_stride;
@@ -610,10 +636,19 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
   ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_next.p, 0, 2 * P.chunks.size() * 4, st));
   ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * P.chunks.size()], st, evf));
+  const cudaStream_t st0 = P.stream;
+  if (P.nsets == 2) {  // fork the second chunk stream off the prologue
+    ADT_CUDA(cudaEventRecord(P.ev_sync[0], st0));
+    ADT_CUDA(cudaStreamWaitEvent(P.stream2, P.ev_sync[0], 0));
+  }
   for (size_t c = 0; c < P.chunks.size(); ++c) {
     const auto& ch = P.chunks[c];
-    BatchArgs<T> Af = make_args<T>(P, ch, (int)(2 * c));
-    BatchArgs<T> Aa = make_args<T>(P, ch, (int)(2 * c + 1));
+    // chunk c: buffer set and stream c % 2 with overlapping chunks.  The set's
+    // previous chunk (c - 2) ran on the same stream, so its buffers are free.
+    const int set = P.nsets == 2 ? (int)(c & 1) : 0;
+    st = set ? P.stream2 : st0;
+    BatchArgs<T> Af = make_args<T>(P, ch, (int)(2 * c), set);
+    BatchArgs<T> Aa = make_args<T>(P, ch, (int)(2 * c + 1), set);
     const int gf = std::min(P.fwd_ctas, ch.count);
     const int ga = std::min(P.adj_ctas, ch.count);
     ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 0], st, evf));
@@ -627,7 +662,7 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
       const double* w = P.d_w.as<double>();
       double* tp = P.d_tpred.as<double>();
       double* sm = P.d_smis.as<double>();
-      unsigned char* scr = P.mis_stride ? P.d_mis_scratch.as<unsigned char>() : nullptr;
+      unsigned char* scr = P.mis_stride ? P.cb[set].mis_scratch.as<unsigned char>() : nullptr;
       int64_t stride = P.mis_stride;
       void* args[] = {&Af, &tobs, &w, &tp, &sm, &scr, &stride};
       ADT_CUDA(cudaLaunchKernel(P.ks.misfit, dim3(ch.count), dim3(256), args, P.mis_smem, st));
@@ -638,10 +673,12 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
       ADT_CUDA(cudaLaunchKernel(P.ks.adj, dim3(ga), dim3(P.adj_warps * 32), args, P.adj_smem, st));
     }
     ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * c + 3], st, evf));
+    // the gradient sums chunks in order (fixed summation order): after chunk c - 1's
+    if (P.nsets == 2 && c > 0) ADT_CUDA(cudaStreamWaitEvent(st, P.ev_sync[c], 0));
     for (int f = 0; f < P.nf; ++f) {
       const int cnt = (int)ch.field_uoff[f].size();
       if (!cnt) continue;
-      const T* lam = P.d_lam.as<T>();
+      const T* lam = P.cb[set].lam.as<T>();
       const int64_t* uo = P.d_uoff.as<int64_t>() + ch.dev_uoff_off[f];
       const double* f64 = P.d_slow64.as<double>() + P.cell_off[f];
       double hh = P.h[f];
@@ -651,7 +688,11 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
       void* args[] = {&lam, &uo, &cc, &f64, &hh, &nc, &gr};
       ADT_CUDA(cudaLaunchKernel(P.ks.grad, dim3(grid1d(nc)), dim3(256), args, 0, st));
     }
+    if (P.nsets == 2) ADT_CUDA(cudaEventRecord(P.ev_sync[c + 1], st));
   }
+  st = st0;
+  if (P.nsets == 2)  // join: the last gradient (on either stream) is done
+    ADT_CUDA(cudaStreamWaitEvent(st0, P.ev_sync[P.chunks.size()], 0));
   if (!P.f64)
     for (int f = 0; f < P.nf; ++f)
       k_grad_scale<<<grid1d(P.geoms[f].ncell), 256, 0, st>>>(

@@ -492,7 +492,8 @@ def run_large(args):
     rng = np.random.default_rng(SEED)
     fields, stations, slow, sf, src, chunk, desc = large_workload(args.workload, rng)
     B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, chunk=chunk,
-                  wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol)
+                  wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
+                  overlap_chunks=bool(args.overlap_chunks))
     n_obs = sum(len(stations[f]) for f in sf)
     B.upload(slow, np.full(n_obs, 1.0), np.ones(n_obs))
     B.run_resident()
@@ -519,6 +520,7 @@ def run_large(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "solves": int(len(sf)), "chunk": chunk,
+                   "overlap_chunks": args.overlap_chunks if chunk else 0,
                    "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
                    "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
                    "cell_updates_per_s": (st.fwd_cell_updates + st.adj_cell_updates) /
@@ -695,7 +697,7 @@ def run_c5_inversion(args):
     sta = synth.surface_stations(m, n, n_sta, rng)
     eve = synth.volume_sources(m, n, l, n_eve, rng)
     opts = dict(tol=1e-6, max_iter=200, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
-                chunk=chunk)
+                chunk=chunk, overlap_chunks=bool(args.overlap_chunks))
     t0 = time.perf_counter()
     P = A.Batch3D([(m, n, l, h)], [sta], np.zeros(n_eve, np.int32), eve, precision=A.ADT_F32,
                   **opts)
@@ -780,6 +782,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=None,
                     help="events timed for the cpu_baseline and compared for error_vs_fp64 "
                          "(0 skips both)")
+    ap.add_argument("--overlap-chunks", type=int, default=1,
+                    help="c5, c5inv: 1 keeps two 128-event chunks resident, the next chunk's "
+                         "forward beside this chunk's adjoint (0: one chunk at a time)")
     ap.add_argument("--c5-fp64-events", type=int, default=128,
                     help="c5inv: events of the FP32-vs-FP64 comparison (0 skips it)")
     ap.add_argument("--c5-fp64-iters", type=int, default=2,

@@ -198,6 +198,10 @@ typedef struct adt_batch_opts {
                            sweeps saw (same fixed point, another iteration path);
                            0: every ordering.  Ignored in FP64, which keeps the
                            reference's iteration path. */
+  int32_t overlap_chunks; /* with several chunks, 1: keep two chunks resident so that
+                           the next chunk's forward runs beside this chunk's adjoint
+                           (twice the chunk memory; same results); 0 (default): one
+                           chunk at a time.  Not with ref_compat. */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;

@@ -444,8 +444,9 @@ def test_batch_run_into_caller_buffers():
 
 
 def test_batch_chunking_and_graph_do_not_change_results():
-    """Chunking, graph replay and launch shapes change only the schedule: the
-    same bits and iteration counts.  The brick depth changes the bricks the
+    """Chunking (one chunk at a time, or two overlapping on two streams), graph
+    replay and launch shapes change only the schedule: the same bits and
+    iteration counts.  The brick depth changes the bricks the
     ordering filters work on: without the forward filter (the adjoint's is
     exact) the results are still the same bits; with it (the FP32 default) the
     forward stops at its tolerance after another iteration path, within 1e-6
@@ -457,7 +458,9 @@ def test_batch_chunking_and_graph_do_not_change_results():
     ref_x = A.Batch3D(fields, stations, sf, src, use_graph=False, fwd_order_filter=False)
     rx = ref_x.run(slow, t_obs, w)
     for kw in ({"chunk": 3}, {"chunk": 1, "use_graph": True}, {"bk": 64}, {"bk": 16}, {"warps": 3},
-               {"warps": 1, "groups": 1}, {"warps": 2, "groups": 5}):
+               {"warps": 1, "groups": 1}, {"warps": 2, "groups": 5},
+               {"chunk": 3, "overlap_chunks": True}, {"chunk": 2, "overlap_chunks": True},
+               {"chunk": 2, "overlap_chunks": True, "use_graph": False}):
         B = A.Batch3D(fields, stations, sf, src, **kw)
         out = B.run(slow, t_obs, w)
         if "bk" in kw:
