@@ -5,8 +5,11 @@
 
 namespace adt {
 
-constexpr int FWD_WPB = 4;     // warps (bricks) per CTA, forward
-constexpr int ADJ_WPB = 2;     // warps per CTA, adjoint
+// Warps (bricks) per CTA.  One: a level has few bricks, and the FP64
+// arithmetic of each brick runs at the rate of one SM's FP64 pipe, so every
+// brick gets an SM of its own.
+constexpr int FWD_WPB = 1;
+constexpr int ADJ_WPB = 1;
 constexpr size_t FWD_WARP_SMEM = (tile_elems(SBK) + itile_elems(SBK)) * sizeof(double);
 constexpr size_t ADJ_WARP_SMEM =
     (2 * tile_elems(SBK) + itile_elems(SBK)) * sizeof(double) + itile_elems(SBK) * sizeof(uint16_t);
