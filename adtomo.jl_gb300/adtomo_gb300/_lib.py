@@ -44,7 +44,8 @@ class BatchOpts(C.Structure):
                 ("warps", C.c_int32), ("groups", C.c_int32), ("use_graph", C.c_int32),
                 ("wake_tol", C.c_double), ("adj_wake_tol", C.c_double),
                 ("adj_order_filter", C.c_int32), ("fwd_order_filter", C.c_int32),
-                ("overlap_chunks", C.c_int32)]
+                ("overlap_chunks", C.c_int32), ("adj_warps", C.c_int32),
+                ("adj_groups", C.c_int32)]
 
 
 class BatchStats(C.Structure):

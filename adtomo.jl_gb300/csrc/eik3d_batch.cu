@@ -206,6 +206,8 @@ void batch_opts_default(adt_batch_opts* o) {
   o->adj_order_filter = 1;
   o->fwd_order_filter = 1;
   o->overlap_chunks = 0;
+  o->adj_warps = 0;
+  o->adj_groups = 0;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -551,7 +553,9 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     P->fwd_regs = fa_f.numRegs;
     P->adj_regs = fa_a.numRegs;
   }
-  if ((rc = apply_shapes(P.get(), o.warps, o.groups, o.warps, o.groups))) return rc;
+  if ((rc = apply_shapes(P.get(), o.warps, o.groups, o.adj_warps ? o.adj_warps : o.warps,
+                          o.adj_groups ? o.adj_groups : o.groups)))
+    return rc;
   int maxsta = 0;
   for (int f = 0; f < n_fields; ++f) maxsta = std::max(maxsta, P->nsta[f]);
   int pw = 1;

@@ -284,9 +284,10 @@ def run_ours(args, rank, world):
     t_obs = gpu_picks(A)
     B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
                   warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
-                  adj_wake_tol=args.adj_wake_tol, fwd_order_filter=bool(args.fwd_order_filter))
+                  adj_wake_tol=args.adj_wake_tol, fwd_order_filter=bool(args.fwd_order_filter),
+                  adj_warps=args.adj_warps, adj_groups=args.adj_groups)
     B.upload([f], t_obs, w)
-    if args.autotune and not (args.warps or args.groups):
+    if args.autotune and not (args.warps or args.groups or args.adj_warps or args.adj_groups):
         B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
     stream = torch.cuda.ExternalStream(B.stream())
     for _ in range(args.warmup):
@@ -419,7 +420,8 @@ def run_ours(args, rank, world):
                    "(1 GB of travel times + 1 GB of adjoint variables per step)",
                    "bk": st.bk, "warps_per_solve": st.warps, "solves_per_cta": st.groups,
                    "adjoint_warps_per_solve": st.adj_warps, "adjoint_solves_per_cta": st.adj_groups,
-                   "shapes": "autotuned" if args.autotune and not (args.warps or args.groups)
+                   "shapes": "autotuned" if args.autotune and not (args.warps or args.groups or
+                                                                args.adj_warps or args.adj_groups)
                    else "fixed",
                    "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
@@ -761,6 +763,9 @@ def main():
     ap.add_argument("--bk", type=int, default=0, help="brick depth (0 = library default)")
     ap.add_argument("--warps", type=int, default=0, help="warps per solve (0 = default)")
     ap.add_argument("--groups", type=int, default=0, help="solves per CTA (0 = as many as fit)")
+    ap.add_argument("--adj-warps", type=int, default=0, help="adjoint warps per solve (0 = --warps)")
+    ap.add_argument("--adj-groups", type=int, default=0,
+                    help="adjoint solves per CTA (0 = --groups)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: time candidate launch shapes on the workload first (untimed setup)")
     ap.add_argument("--workload", default="c3",

@@ -202,6 +202,8 @@ typedef struct adt_batch_opts {
                            the next chunk's forward runs beside this chunk's adjoint
                            (twice the chunk memory; same results); 0 (default): one
                            chunk at a time.  Not with ref_compat. */
+  int32_t adj_warps;    /* adjoint kernel's warps per solve: 0 = as `warps` */
+  int32_t adj_groups;   /* adjoint kernel's solves per CTA: 0 = as `groups` */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;
