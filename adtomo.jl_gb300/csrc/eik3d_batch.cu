@@ -462,7 +462,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   }
   R_(P->d_nseed, (size_t)n_solves * 4);
   R_(P->d_next, (size_t)2 * P->chunks.size() * 4);
-  R_(P->d_counters, 6 * 8);
+  R_(P->d_counters, 4 * 8);
   // level lists per field
   std::vector<uint32_t> lv;
   std::vector<int> ls;
@@ -639,7 +639,7 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
                                                      P.src_vel ? 1 : 0,
                                                      P.d_cost.as<unsigned long long>());
   ADT_CUDA(cudaMemsetAsync(P.d_grad.p, 0, P.ncell_total * 8, st));
-  ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 6 * 8, st));
+  ADT_CUDA(cudaMemsetAsync(P.d_counters.p, 0, 4 * 8, st));
   ADT_CUDA(cudaMemsetAsync(P.d_next.p, 0, 2 * P.chunks.size() * 4, st));
   ADT_CUDA(cudaEventRecordWithFlags(P.ev[4 * P.chunks.size()], st, evf));
   const cudaStream_t st0 = P.stream;
@@ -853,14 +853,12 @@ int batch_stats(BatchPlan* P, adt_batch_stats* s) {
   s->fwd_ms = s->adj_ms = s->total_ms = -1.f;
   if (!P->ran) return ADT_OK;
   ADT_CUDA(cudaStreamSynchronize(P->stream));
-  unsigned long long c[6];
+  unsigned long long c[4];
   ADT_CUDA(cudaMemcpy(c, P->d_counters.p, sizeof c, cudaMemcpyDeviceToHost));
   s->fwd_cell_updates = (int64_t)c[0];
   s->fwd_bricks = (int64_t)c[1];
   s->adj_cell_updates = (int64_t)c[2];
   s->adj_bricks = (int64_t)c[3];
-  s->adj_dag_bricks = (int64_t)c[4];
-  s->adj_fallback_solves = (int64_t)c[5];
   float fw = 0.f, aw = 0.f, tot = 0.f, t;
   for (size_t ch = 0; ch < P->chunks.size(); ++ch) {
     ADT_CUDA(cudaEventElapsedTime(&t, P->ev[4 * ch], P->ev[4 * ch + 1]));

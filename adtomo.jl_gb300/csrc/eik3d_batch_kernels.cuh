@@ -72,8 +72,6 @@ struct BatchArgs {
   int* next;                // work counter
   adt_solve_status* status; // per global solve
   unsigned long long* counters;  // [0] fwd cell updates [1] fwd bricks [2] adj updates [3] adj bricks
-                                 // [4] bricks final after the adjoint's dependency pass
-                                 // [5] solves it left to the iterative sweeps
   unsigned long long* cost;  // per solve: bricks swept in this evaluation (orders the next one)
   double tol;
   float wake;               // FP32 forward: decrease at or below which a brick wakes no one
@@ -98,9 +96,9 @@ struct GroupShared {
   unsigned long long err;
   int lo[2], hi[2];  // level range with pending bricks at the start of an ordering (run_ordering)
   int lchg[3];       // a brick of level d changed in this ordering: lchg[d % 3]
-  // adjoint dependency pass: queue head and tail, bricks final, bricks taken
-  // from the queue and finished with, and a flag for a wait that ran out
-  int dq_head, dq_tail, dn_done, dn_fin, dag_err;
+  // adjoint dependency pass (adjoint_dag): queue head and tail, bricks done,
+  // warps holding a brick, and a flag for a wait that ran out
+  int dq_head, dq_tail, dn_done, dn_busy, dag_err;
 };
 
 // Empty level ranges for both orderings' slots (run_ordering), at the start
@@ -981,7 +979,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     }
     if (c.gw == 0 && lane == 0) {
       group_reset_range(gs);
-      gs->dq_head = gs->dq_tail = gs->dn_done = gs->dn_fin = gs->dag_err = 0;
+      gs->dq_head = gs->dq_tail = gs->dn_done = gs->dn_busy = gs->dag_err = 0;
     }
     group_sync(c.grp, c.gthreads);
     // pass 2: users (reads only the low bits of neighbours, writes own high bits);
@@ -1110,6 +1108,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
       for (;;) {
         int slot = -1;
         if (lane == 0) {
+          atomicAdd(&gs->dn_busy, 1);  // announced before looking, withdrawn if nothing found
           int h = ((volatile int*)&gs->dq_head)[0];
           while (h < ((volatile int*)&gs->dq_tail)[0]) {
             const int prev = atomicCAS(&gs->dq_head, h, h + 1);
@@ -1119,6 +1118,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
             }
             h = prev;
           }
+          if (slot < 0) atomicSub(&gs->dn_busy, 1);
         }
         slot = __shfl_sync(0xffffffffu, slot, 0);
         if (slot >= 0) {
@@ -1198,24 +1198,21 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
             }
           }
           __syncwarp();
-          if (lane == 0) {  // after this brick's releases
+          if (lane == 0) {
             __threadfence_block();
-            atomicAdd(&gs->dn_fin, 1);
+            atomicSub(&gs->dn_busy, 1);
           }
           continue;
         }
-        // Nothing to take.  A brick is pushed before the brick that releases
-        // it counts as finished, so tail - fin counts the bricks queued or in
-        // hand; fin read first and then tail equal means none was at the
-        // moment tail was read, and none can appear again: quiescent (all
-        // final, or the rest waits on a cycle).
+        // nothing to take: all final, no warp left that could release more,
+        // or a wait ran out
         int st = 0;
         if (lane == 0) {
-          const int fin = ((volatile int*)&gs->dn_fin)[0];
-          __threadfence_block();
-          const int tail = ((volatile int*)&gs->dq_tail)[0];
-          if (fin >= tail) {
+          if (((volatile int*)&gs->dn_done)[0] >= nb) {
             st = 1;
+          } else if (((volatile int*)&gs->dn_busy)[0] == 0 &&
+                     ((volatile int*)&gs->dq_head)[0] >= ((volatile int*)&gs->dq_tail)[0]) {
+            st = 2;
           } else if (((volatile int*)&gs->dag_err)[0] || ++idle > DAG_WAIT_LIMIT) {
             atomicExch(&gs->dag_err, 1);
             st = 3;
@@ -1226,12 +1223,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         if (__shfl_sync(0xffffffffu, st, 0)) break;
       }
       group_sync(c.grp, c.gthreads);
-      const int ndone = ((volatile int*)&gs->dn_done)[0];
-      dag_all = ndone >= nb;
-      if (c.gw == 0 && lane == 0) {
-        atomicAdd(&A.counters[4], (unsigned long long)ndone);
-        if (!dag_all) atomicAdd(&A.counters[5], 1ull);
-      }
+      dag_all = ((volatile int*)&gs->dn_done)[0] >= nb;
       group_sync(c.grp, c.gthreads);
       if (!dag_all) {  // the iterative sweeps start from the final bricks
         for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {

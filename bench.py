@@ -425,8 +425,6 @@ def run_ours(args, rank, world):
                    else "fixed",
                    "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
-                   "adj_dag_bricks": int(st.adj_dag_bricks),
-                   "adj_fallback_solves": int(st.adj_fallback_solves),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
                    "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
                    "fwd_order_filter": args.fwd_order_filter, "adj_dag": args.adj_dag,

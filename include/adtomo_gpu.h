@@ -275,8 +275,6 @@ typedef struct adt_batch_stats {
   int32_t ctas;
   int32_t adj_warps;  /* the same for the adjoint kernel */
   int32_t adj_groups;
-  int64_t adj_dag_bricks;      /* bricks final after the adjoint's dependency pass */
-  int64_t adj_fallback_solves; /* solves the dependency pass left to the iterative sweeps */
 } adt_batch_stats;
 int adt_batch_stats_get(adt_batch* b, adt_batch_stats* out);
 
