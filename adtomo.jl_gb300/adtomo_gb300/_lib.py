@@ -45,7 +45,7 @@ class BatchOpts(C.Structure):
                 ("wake_tol", C.c_double), ("adj_wake_tol", C.c_double),
                 ("adj_order_filter", C.c_int32), ("fwd_order_filter", C.c_int32),
                 ("overlap_chunks", C.c_int32), ("adj_warps", C.c_int32),
-                ("adj_groups", C.c_int32), ("adj_dag", C.c_int32)]
+                ("adj_groups", C.c_int32)]
 
 
 class BatchStats(C.Structure):

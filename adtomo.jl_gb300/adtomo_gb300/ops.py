@@ -131,7 +131,7 @@ class Batch3D:
                  max_iter=200, adj_max_iter=200, ref_compat=False, near_src_f64=2, chunk=0,
                  bk=0, warps=0, groups=0, use_graph=True, wake_tol=0.0, adj_wake_tol=0.0,
                  adj_order_filter=True, fwd_order_filter=True, overlap_chunks=False,
-                 adj_warps=0, adj_groups=0, adj_dag=True):
+                 adj_warps=0, adj_groups=0):
         L = lib()
         self._L = L
         self.fields = [tuple(x) for x in fields]
@@ -155,7 +155,6 @@ class Batch3D:
         o.fwd_order_filter = int(bool(fwd_order_filter))
         o.overlap_chunks = int(bool(overlap_chunks))
         o.adj_warps, o.adj_groups = adj_warps, adj_groups
-        o.adj_dag = int(bool(adj_dag))
         self._keep = (dims, hs, sta, src)
         h = C.c_void_p()
         check(L.adt_batch_create(C.byref(h), len(self.fields), _ptr(dims), _ptr(hs),

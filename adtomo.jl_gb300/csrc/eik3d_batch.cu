@@ -208,7 +208,6 @@ void batch_opts_default(adt_batch_opts* o) {
   o->overlap_chunks = 0;
   o->adj_warps = 0;
   o->adj_groups = 0;
-  o->adj_dag = 1;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -620,7 +619,6 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.max_nb = P.max_nb;
   A.adj_order_filter = P.opts.adj_order_filter ? 1 : 0;
   A.fwd_order_filter = (!P.f64 && P.opts.fwd_order_filter) ? 1 : 0;
-  A.adj_dag = P.opts.adj_dag ? 1 : 0;
   return A;
 }
 

@@ -86,7 +86,6 @@ struct BatchArgs {
   int adj_order_filter;     // 1: adjoint sweeps a brick only in the orderings its flow allows
   int fwd_order_filter;     // 1: FP32 forward sweeps a brick only in the orderings its
                             //    learned upwind directions allow
-  int adj_dag;              // 1: adjoint dependency pass before the iterative sweeps
 };
 
 // Per-group scalars at the start of dynamic shared memory.
@@ -96,9 +95,6 @@ struct GroupShared {
   unsigned long long err;
   int lo[2], hi[2];  // level range with pending bricks at the start of an ordering (run_ordering)
   int lchg[3];       // a brick of level d changed in this ordering: lchg[d % 3]
-  // adjoint dependency pass (adjoint_dag): queue head and tail, bricks done,
-  // warps holding a brick, and a flag for a wait that ran out
-  int dq_head, dq_tail, dn_done, dn_busy, dag_err;
 };
 
 // Empty level ranges for both orderings' slots (run_ordering), at the start
@@ -119,22 +115,8 @@ __device__ __forceinline__ void group_sync(int grp, int nthreads) {
 // learned upwind directions (fmask, run_ordering).  The global meta buffer
 // holds META_ARRAYS_MAX arrays per solve.
 constexpr int META_ARRAYS_FWD = 3;
-constexpr int META_ARRAYS_ADJ = 4;
-constexpr int META_ARRAYS_MAX = 4;
-
-// The adjoint's per-brick word (`info`, its third metadata array):
-//   bits 0-5   flow: OR of the user bits of the brick's cells (x-, x+, y-, y+, z-, z+)
-//   bits 8-13  inflow faces: a cell on that face is used by the cell across it,
-//              so the brick across the face feeds this one
-//   bit 14     the brick's adjoint values are not all zero (dependency pass)
-//   bit 15     the brick is final (dependency pass)
-//   bits 16-18 feeding neighbours not yet final (dependency pass)
-// and its fourth array is the dependency pass's queue of ready bricks.
-constexpr int INFO_FLOW = 63;
-constexpr int INFO_FACE_SHIFT = 8;
-constexpr int INFO_NZ = 1 << 14;
-constexpr int INFO_DONE = 1 << 15;
-constexpr int INFO_INDEG_SHIFT = 16;
+constexpr int META_ARRAYS_ADJ = 3;
+constexpr int META_ARRAYS_MAX = 3;
 
 // Dynamic shared memory: [G GroupShared][G * narr * max_nb meta ints][warp tiles]
 __host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_nb, int narr) {
@@ -333,7 +315,7 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
   // does brick b need a sweep at level time t (dirty, and allowed by the filters)?
   auto pending = [&](int b, int bx, int by, int bz, int t) -> bool {
     if (flow) {
-      const int fl = ((const volatile int*)flow)[b] & 63;
+      const int fl = ((const volatile int*)flow)[b];
       return adjoint_flow_allowed(fl, forbid) && brick_dirty(mod, proc, g, b, bx, by, bz, t, fl);
     }
     if (fmask) {
@@ -824,11 +806,9 @@ __device__ __forceinline__ void adj_pass1_vec4(const float* u, uint16_t* code, f
 
 // User bits of four consecutive cells (pass 2) from 8-byte loads of the
 // codes: neighbour r uses c when r is not fixed and its upwind side along
-// the axis points at c.  Returns the OR of the four cells' user bits, with
-// bit 6 set when one of them lies on the z- face of its brick (depth bk) and
-// is used across it, bit 7 likewise for the z+ face.
+// the axis points at c.  Returns the OR of the four cells' user bits.
 __device__ __forceinline__ uint32_t adj_pass2_vec4(uint16_t* code, const Geom& g, int64_t x,
-                                                   int i, int j, int k, int bk) {
+                                                   int i, int j, int k) {
   const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
   auto ld4 = [&](int64_t y) -> uint2 { return *reinterpret_cast<const uint2*>(code + y); };
   auto c16 = [](uint2 v, int q) -> uint32_t {
@@ -860,8 +840,6 @@ __device__ __forceinline__ uint32_t adj_pass2_vec4(uint16_t* code, const Geom& g
       if (uses(q == 3 ? zp : c16(c4, q + 1), 2, 1u)) us |= 32u;
       cd |= us << CODE_USERS;
       all |= us;
-      if ((us & 16u) && (k + q) % bk == 0) all |= 64u;
-      if ((us & 32u) && (k + q + 1) % bk == 0) all |= 128u;
     }
     packed[q >> 1] |= cd << (16 * (q & 1));
   }
@@ -890,30 +868,6 @@ __device__ __forceinline__ bool dispatch_adj_f32(const float* U, float* L, const
 #undef ADT_ADJ_CASE
 }
 
-// Absolute brick coordinates to a brick position (no mirroring).
-template <int BK>
-__device__ __forceinline__ BrickPos brick_pos_abs(const Geom& g, int bx, int by, int bz) {
-  BrickPos p;
-  p.bx = bx;
-  p.by = by;
-  p.bz = bz;
-  p.i0 = bx * BI;
-  p.j0 = by * BJ;
-  p.k0 = bz * BK;
-  p.ni = min(BI, g.m - p.i0);
-  p.nj = min(BJ, g.n - p.j0);
-  p.nk = min(BK, g.l - p.k0);
-  return p;
-}
-
-// Rounds of sweeps over its allowed orderings a brick with flow both ways
-// along an axis gets in the dependency pass before it is left to the
-// iterative sweeps.
-constexpr int DAG_ROUNDS = 32;
-// Bound of every wait of the dependency pass (polls with a short sleep):
-// reaching it sets dag_err, and the solve falls back to the iterative sweeps.
-constexpr int DAG_WAIT_LIMIT = 1 << 22;
-
 template <class T, int BK>
 __global__ void k_batch_adj(BatchArgs<T> A) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -926,7 +880,6 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
   uint16_t* C = reinterpret_cast<uint16_t*>(L + tile_elems(BK));
   unsigned long long cnt_upd = 0, cnt_brk = 0;
   constexpr bool EXACT = sizeof(T) == 8;
-  GroupShared* gs = c.gs;
   bool first = true;
   for (;;) {
     const int q = group_next(A, c, first);
@@ -940,11 +893,9 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     T* lam = A.lam + sd.u_off;
     uint16_t* code = A.code + sd.u_off;
     const int nb = g.nbx * g.nby * g.nbz;
-    const int mstride = c.smeta ? A.max_nb : nb;
     int* mod = c.smeta ? c.smeta : A.meta + sd.meta_off;
-    int* proc = mod + mstride;
-    int* info = proc + mstride;
-    int* dqueue = info + mstride;
+    int* proc = mod + (c.smeta ? A.max_nb : nb);
+    int* flow = proc + (c.smeta ? A.max_nb : nb);
     const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
     const bool vec = (g.l % 8) == 0;
     // pass 1: upwind sides and fixed cells; lambda = 0
@@ -974,36 +925,23 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
       mod[b] = -2;
       proc[b] = -1;
-      info[b] = 0;
-      dqueue[b] = 0;
+      flow[b] = 0;
     }
-    if (c.gw == 0 && lane == 0) {
-      group_reset_range(gs);
-      gs->dq_head = gs->dq_tail = gs->dn_done = gs->dn_busy = gs->dag_err = 0;
-    }
+    if (c.gw == 0 && lane == 0) group_reset_range(c.gs);
     group_sync(c.grp, c.gthreads);
     // pass 2: users (reads only the low bits of neighbours, writes own high bits);
-    // each brick's info collects its cells' user bits (flow) and the faces
-    // whose cells are used across them (inflow faces)
-    auto add_info = [&](int i, int j, int k, uint32_t us, uint32_t zfaces) {
-      us &= 63u;
+    // each brick's flow collects its cells' user bits
+    auto add_flow = [&](int i, int j, int k, uint32_t us) {
       if (!us) return;
-      uint32_t faces = zfaces;
-      if ((us & 1u) && i % BI == 0) faces |= 1u;
-      if ((us & 2u) && (i + 1) % BI == 0) faces |= 2u;
-      if ((us & 4u) && j % BJ == 0) faces |= 4u;
-      if ((us & 8u) && (j + 1) % BJ == 0) faces |= 8u;
-      const int w = (int)(us | (faces << INFO_FACE_SHIFT));
-      int* fb = info + ((i / BI) * g.nby + (j / BJ)) * g.nbz + (k / BK);
-      if ((((const volatile int*)fb)[0] & w) != w) atomicOr(fb, w);
+      int* fb = flow + ((i / BI) * g.nby + (j / BJ)) * g.nbz + (k / BK);
+      if ((((const volatile int*)fb)[0] & (int)us) != (int)us) atomicOr(fb, (int)us);
     };
     if constexpr (sizeof(T) == 4) {
       if (vec4)
         for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += c.gthreads) {
           const int64_t col = e / (g.l / 4);
           const int i = (int)(col / g.n), j = (int)(col % g.n), k = (int)(4 * e - col * g.l);
-          const uint32_t r = adj_pass2_vec4(code, g, 4 * e, i, j, k, BK);
-          add_info(i, j, k, r, ((r >> 6) & 3u) << 4);
+          add_flow(i, j, k, adj_pass2_vec4(code, g, 4 * e, i, j, k));
         }
     }
     for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
@@ -1024,10 +962,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         if (k > 0 && uses(x - 1, 2, 2)) us |= 16;
         if (k < g.l - 1 && uses(x + 1, 2, 1)) us |= 32;
         code[x] = (uint16_t)(cd | (us << CODE_USERS));
-        uint32_t zf = 0;
-        if ((us & 16) && k % BK == 0) zf |= 16u;
-        if ((us & 32) && (k + 1) % BK == 0) zf |= 32u;
-        add_info(i, j, k, us, zf);
+        add_flow(i, j, k, us);
       }
     }
     group_sync(c.grp, c.gthreads);
@@ -1044,217 +979,59 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
       mod[((i / BI) * g.nby + (j / BJ)) * g.nbz + (k / BK)] = -1;
     }
     group_sync(c.grp, c.gthreads);
-
-    // One sweep of brick p in ordering (si, sj, sk): stage, sweep, write back.
-    // Returns whether any adjoint value changed; sig: whether one changed by
-    // more than eps relative (FP32; eps = 0 makes it the same).
-    auto adj_sweep = [&](const BrickPos& p, int si, int sj, int sk, float eps, bool& sig) -> bool {
-      const int CS = tile_col_stride(BK, sj == sk);
-      bool ch;
-      if constexpr (sizeof(T) == 4) {
-        if (vec) {
-          load_tile_f32_async<BK>(U, u, g, p, CS, lane);
-          load_tile_f32_async<BK>(L, lam, g, p, CS, lane, 0.0f);
-          const bool seeds = load_codes_vec<BK>(C, code, g, p, CS, lane);
-          cp_async_wait_all();
-          __syncwarp();
-          ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane, eps,
-                                    seeds, sig);
-          if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
-          return ch;
-        }
-      }
-      load_halo_tile<T, BK>(U, u, g, p, CS, lane);
-      load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
-      load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
-      cp_async_wait_all();
-      __syncwarp();
-      ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si, sj, sk,
-                                                CS, lane);
-      if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
-      sig = ch;
-      return ch;
-    };
-
-    // Dependency pass.  The adjoint system is triangular, and so, mostly, is
-    // its brick-level structure: a brick's adjoint values depend only on its
-    // own seeds and on the bricks that feed it through its inflow faces.  A
-    // brick whose feeders are final is swept to its own final values once:
-    // one sweep in the ordering that follows its flow when every axis flows
-    // one way, repeated rounds over its allowed orderings otherwise.  Warps
-    // take ready bricks from a queue in shared (or global) memory; a final
-    // brick releases the bricks it feeds.  Bricks with no seed and no
-    // nonzero feeder stay zero without a sweep.  What cannot be ordered this
-    // way (bricks that feed each other through a face carrying flow both
-    // ways, and what depends on them) is left to the iterative sweeps below,
-    // which start from the final bricks.  Exact: the order only schedules
-    // Gauss-Seidel updates toward the system's unique solution.
-    bool dag_all = false;
-    if (A.adj_dag) {
-      const int sYZ = g.nby * g.nbz;
-      for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
-        const int faces = (info[b] >> INFO_FACE_SHIFT) & 63;
-        const int d = __popc(faces);
-        if (d) {
-          atomicAdd(&info[b], d << INFO_INDEG_SHIFT);
-        } else {
-          const int t = atomicAdd(&gs->dq_tail, 1);
-          ((volatile int*)dqueue)[t] = b + 1;
-        }
-      }
-      __threadfence_block();
-      group_sync(c.grp, c.gthreads);
-      int idle = 0;
-      for (;;) {
-        int slot = -1;
-        if (lane == 0) {
-          atomicAdd(&gs->dn_busy, 1);  // announced before looking, withdrawn if nothing found
-          int h = ((volatile int*)&gs->dq_head)[0];
-          while (h < ((volatile int*)&gs->dq_tail)[0]) {
-            const int prev = atomicCAS(&gs->dq_head, h, h + 1);
-            if (prev == h) {
-              slot = h;
-              break;
-            }
-            h = prev;
-          }
-          if (slot < 0) atomicSub(&gs->dn_busy, 1);
-        }
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot >= 0) {
-          idle = 0;
-          int b = -1;
-          if (lane == 0) {  // the pusher reserved the slot before writing it
-            for (int w = 0; w < DAG_WAIT_LIMIT; ++w) {
-              const int e = ((volatile int*)dqueue)[slot];
-              if (e) {
-                b = e - 1;
-                break;
-              }
-              __nanosleep(32);
-            }
-            if (b < 0) atomicExch(&gs->dag_err, 1);
-          }
-          b = __shfl_sync(0xffffffffu, b, 0);
-          if (b >= 0) {
-            __threadfence_block();  // after the feeders' adjoint values
-            const int inf = ((volatile int*)info)[b];
-            const int fl = inf & INFO_FLOW, faces = (inf >> INFO_FACE_SHIFT) & 63;
-            const int bx = b / sYZ, by = (b / g.nbz) % g.nby, bz = b % g.nbz;
-            const int nbr[6] = {b - sYZ, b + sYZ, b - g.nbz, b + g.nbz, b - 1, b + 1};
-            bool need = ((volatile int*)mod)[b] == -1;  // seeded
-            for (int f = 0; f < 6 && !need; ++f)
-              if ((faces >> f) & 1) need = (((volatile int*)info)[nbr[f]] & INFO_NZ) != 0;
-            bool ok = true;
-            if (need) {
-              // every axis flows one way: one sweep in the ordering that follows
-              // the flow is final; otherwise rounds over the allowed orderings
-              // until one changes nothing
-              const BrickPos p = brick_pos_abs<BK>(g, bx, by, bz);
-              const unsigned long long cells = (unsigned long long)p.ni * p.nj * p.nk;
-              const bool mixed = (fl & (fl >> 1) & 0x15) != 0;
-              ok = !mixed;
-              bool any = false;
-              int o = -1, rounds = 0;
-              for (;;) {
-                int si = (fl & 2) ? -1 : 1, sj = (fl & 8) ? -1 : 1, sk = (fl & 32) ? -1 : 1;
-                if (mixed) {  // next allowed ordering; a full round without a change ends
-                  do {
-                    if (++o == 8) {
-                      o = 0;
-                      if (!any) ok = true;
-                      any = false;
-                      ++rounds;
-                    }
-                    ordering3(o, si, sj, sk);
-                  } while (!adjoint_flow_allowed(fl, adjoint_flow_forbidden(si, sj, sk)));
-                  if (ok || rounds >= DAG_ROUNDS) break;
-                }
-                bool sig;
-                any |= adj_sweep(p, si, sj, sk, 0.0f, sig);
-                cnt_upd += cells;
-                cnt_brk += 1;
-                if (!mixed) break;
-              }
-            }
-            __threadfence_block();  // this brick's adjoint values before its release
-            __syncwarp();
-            if (lane == 0 && ok) {
-              atomicOr(&info[b], INFO_DONE | (need ? INFO_NZ : 0));
-              const bool in[6] = {bx > 0, bx < g.nbx - 1, by > 0, by < g.nby - 1, bz > 0,
-                                  bz < g.nbz - 1};
-              for (int f = 0; f < 6; ++f) {
-                if (!in[f]) continue;
-                const int n = nbr[f];
-                // n is fed by b when n's face toward b (the opposite face) is an inflow face
-                if (!((((volatile int*)info)[n] >> (INFO_FACE_SHIFT + (f ^ 1))) & 1)) continue;
-                const int old = atomicSub(&info[n], 1 << INFO_INDEG_SHIFT);
-                if (((old >> INFO_INDEG_SHIFT) & 7) == 1) {
-                  const int t = atomicAdd(&gs->dq_tail, 1);
-                  ((volatile int*)dqueue)[t] = n + 1;
-                }
-              }
-              atomicAdd(&gs->dn_done, 1);
-            }
-          }
-          __syncwarp();
-          if (lane == 0) {
-            __threadfence_block();
-            atomicSub(&gs->dn_busy, 1);
-          }
-          continue;
-        }
-        // nothing to take: all final, no warp left that could release more,
-        // or a wait ran out
-        int st = 0;
-        if (lane == 0) {
-          if (((volatile int*)&gs->dn_done)[0] >= nb) {
-            st = 1;
-          } else if (((volatile int*)&gs->dn_busy)[0] == 0 &&
-                     ((volatile int*)&gs->dq_head)[0] >= ((volatile int*)&gs->dq_tail)[0]) {
-            st = 2;
-          } else if (((volatile int*)&gs->dag_err)[0] || ++idle > DAG_WAIT_LIMIT) {
-            atomicExch(&gs->dag_err, 1);
-            st = 3;
-          } else {
-            __nanosleep(64);
-          }
-        }
-        if (__shfl_sync(0xffffffffu, st, 0)) break;
-      }
-      group_sync(c.grp, c.gthreads);
-      dag_all = ((volatile int*)&gs->dn_done)[0] >= nb;
-      group_sync(c.grp, c.gthreads);
-      if (!dag_all) {  // the iterative sweeps start from the final bricks
-        for (int b = c.gw * 32 + lane; b < nb; b += c.gthreads) {
-          mod[b] = (info[b] & INFO_DONE) ? -2 : -1;
-          proc[b] = -1;
-        }
-        group_sync(c.grp, c.gthreads);
-      }
-    }
-    int it = 0;
-    bool conv = dag_all;
-    for (it = 0; !dag_all && it < A.adj_max_iter; ++it) {
-      if (c.gw == 0 && lane == 0) gs->changed = 0;
+    int it;
+    bool conv = false;
+    for (it = 0; it < A.adj_max_iter; ++it) {
+      if (c.gw == 0 && lane == 0) c.gs->changed = 0;
       group_sync(c.grp, c.gthreads);
       bool any = false;
       for (int o = 0; o < 8; ++o) {
         int si, sj, sk;
         ordering3(o, si, sj, sk);
-        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, A.adj_order_filter ? info : nullptr,
+        const int CS = tile_col_stride(BK, sj == sk);
+        run_ordering<BK>(c, g, fd.bricks, fd.lstart, mod, proc, A.adj_order_filter ? flow : nullptr,
                          nullptr, (it * 8 + o) * g.nlev, si, sj, sk, cnt_upd, cnt_brk,
                          [&](const BrickPos& p, uint32_t&) -> bool {
-          bool sig;
-          adj_sweep(p, si, sj, sk, A.adj_wake, sig);
-          // only a significant change wakes neighbours and extends the solve
-          any |= sig;
-          return sig;
+          bool ch;
+          if constexpr (sizeof(T) == 4) {
+            if (vec) {
+              load_tile_f32_async<BK>(U, u, g, p, CS, lane);
+              load_tile_f32_async<BK>(L, lam, g, p, CS, lane, 0.0f);
+              const bool seeds = load_codes_vec<BK>(C, code, g, p, CS, lane);
+              cp_async_wait_all();
+              __syncwarp();
+              bool sig;
+              ch = dispatch_adj_f32<BK>(U, L, C, A.gdense + sd.u_off, g, p, si, sj, sk, lane,
+                                        A.adj_wake, seeds, sig);
+              if (ch) store_interior_f32_vec<BK>(L, lam, g, p, CS, lane);
+              ch = sig;  // only a significant change wakes neighbours and extends the solve
+            } else {
+              load_halo_tile<T, BK>(U, u, g, p, CS, lane);
+              load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
+              load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
+              cp_async_wait_all();
+              __syncwarp();
+              ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si,
+                                                        sj, sk, CS, lane);
+              if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+            }
+          } else {
+            load_halo_tile<T, BK>(U, u, g, p, CS, lane);
+            load_halo_tile<T, BK>(L, lam, g, p, CS, lane);
+            load_interior<uint16_t, BK>(C, code, g, p, CS, lane);
+            cp_async_wait_all();
+            __syncwarp();
+            ch = sweep_brick_adj<T, BK, EXACT, false>(U, L, C, nullptr, sidx, sval, ns, g, p, si,
+                                                      sj, sk, CS, lane);
+            if (ch) store_interior<T, BK>(L, lam, g, p, CS, lane);
+          }
+          any |= ch;
+          return ch;
         });
       }
-      if (any && lane == 0) gs->changed = 1;
+      if (any && lane == 0) c.gs->changed = 1;
       group_sync(c.grp, c.gthreads);
-      const bool changed = gs->changed != 0;
+      const bool changed = c.gs->changed != 0;
       group_sync(c.grp, c.gthreads);
       if (!changed) {
         conv = true;
@@ -1266,8 +1043,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     if (lane == 0 && cnt_brk > brk0) atomicAdd(&A.cost[sd.gidx], cnt_brk - brk0);
     if (c.gw == 0 && lane == 0) {
       adt_solve_status& st = A.status[sd.gidx];
-      // the dependency pass counts as one iteration
-      st.adj_iters = (A.adj_dag ? 1 : 0) + (dag_all ? 0 : (conv ? it + 1 : it));
+      st.adj_iters = conv ? it + 1 : it;
       st.adj_converged = conv ? 1 : 0;
     }
   }

@@ -285,7 +285,7 @@ def run_ours(args, rank, world):
     B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
                   warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
                   adj_wake_tol=args.adj_wake_tol, fwd_order_filter=bool(args.fwd_order_filter),
-                  adj_warps=args.adj_warps, adj_groups=args.adj_groups, adj_dag=bool(args.adj_dag))
+                  adj_warps=args.adj_warps, adj_groups=args.adj_groups)
     B.upload([f], t_obs, w)
     if args.autotune and not (args.warps or args.groups or args.adj_warps or args.adj_groups):
         B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
@@ -382,7 +382,7 @@ def run_ours(args, rank, world):
         k = cpu_sample
         E = A.Batch3D([(M, N, L, H)], [sta], np.zeros(k, np.int32), src[:k], precision=A.ADT_F32,
                       tol=1e-6, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
-                      fwd_order_filter=bool(args.fwd_order_filter), adj_dag=bool(args.adj_dag))
+                      fwd_order_filter=bool(args.fwd_order_filter))
         mis_k, tp_k, (g_k,), _ = E.run([f], t_obs[:k * N_STA], w[:k * N_STA])
         E.close()
         mo, tpo, go = cpu_out
@@ -427,7 +427,7 @@ def run_ours(args, rank, world):
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
                    "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
-                   "fwd_order_filter": args.fwd_order_filter, "adj_dag": args.adj_dag,
+                   "fwd_order_filter": args.fwd_order_filter,
                    "picks": "FP64 travel times on the +2%-noise model (reference stopping rule)",
                    "vs_exact_skipping": vs_exact, "error_vs_fp64": err64},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
@@ -782,8 +782,6 @@ def main():
     ap.add_argument("--fwd-order-filter", type=int, default=1,
                     help="1 (library default): FP32 forward sweeps each brick only in the "
                          "orderings that follow its learned upwind directions; 0: all")
-    ap.add_argument("--adj-dag", type=int, default=1,
-                    help="1 (library default): adjoint dependency pass before the iterative sweeps")
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="events timed through the plain FP64 single-event path (0 skips)")
     ap.add_argument("--cpu-sample", type=int, default=None,

@@ -204,10 +204,6 @@ typedef struct adt_batch_opts {
                            chunk at a time.  Not with ref_compat. */
   int32_t adj_warps;    /* adjoint kernel's warps per solve: 0 = as `warps` */
   int32_t adj_groups;   /* adjoint kernel's solves per CTA: 0 = as `groups` */
-  int32_t adj_dag;      /* 1 (default): the adjoint first sweeps each brick once its
-                           feeding bricks are final (a dependency order over the bricks;
-                           exact), the iterative sweeps finish what it cannot order;
-                           0: iterative sweeps only */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;
