@@ -31,8 +31,11 @@ __host__ __device__ __forceinline__ T rmax(T a, T b) {
 // column, BK cells deep along k (the contiguous axis).
 constexpr int BI = 8;
 constexpr int BJ = 4;
-// Brick depth of the plain single-solve 3D path (the batched plan chooses its own).
-constexpr int SBK = 32;
+// Brick depth of the plain single-solve 3D path (the batched plan chooses its
+// own).  16: a level of one solve holds few bricks, each on its own SM, and a
+// level lasts one brick's chain of FP64 steps (16 + 10 steps, against 42 for
+// 32 cells).
+constexpr int SBK = 16;
 
 // Shared-memory tile of one brick with a one-cell halo on every side:
 // column (pi, pj) for pi in [-1, BI], pj in [-1, BJ]; slot k+1 for k in

@@ -5,6 +5,10 @@
 //    round-to-nearest intrinsics (__dmul_rn, __dadd_rn, __ddiv_rn, __dsqrt_rn),
 //    which the compiler never contracts into FMAs, so results are bit-identical
 //    to the reference compiled for x86-64 (Eikonal.h:14-20, Eikonal3D.cpp:11-28).
+//    A division by 2.0 is written as a multiplication by 0.5: both are the
+//    correctly rounded value of the same exact quotient, so the bits are the
+//    same, and the multiplication is one instruction where the division is a
+//    long dependent sequence in FP64.
 //  * upd3_stable<T>: the same roots written without the B^2 - 4C cancellation:
 //      two-term:   x = a + (d2 + sqrt(2 F^2 - d2^2)) / 2,           d2 = b - a
 //      three-term: x = a + (d2 + d3 + sqrt(3 F^2 - d2^2 - d3^2 - (d3-d2)^2)) / 3
@@ -25,14 +29,14 @@ __device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, do
   if (x <= a2) return x;
   const double ffhh = __dmul_rn(__dmul_rn(__dmul_rn(f, f), h), h);
   double B = -__dadd_rn(a1, a2);
-  double C = __ddiv_rn(__dsub_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), ffhh), 2.0);
-  x = __ddiv_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 2.0);
+  double C = __dmul_rn(__dsub_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), ffhh), 0.5);
+  x = __dmul_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
   if (x <= a3) return x;
   B = __ddiv_rn(__dmul_rn(-2.0, __dadd_rn(__dadd_rn(a1, a2), a3)), 3.0);
   C = __ddiv_rn(
       __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), __dmul_rn(a3, a3)), ffhh),
       3.0);
-  return __ddiv_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 2.0);
+  return __dmul_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
 }
 
 // Two-term update, reference arithmetic (Eikonal.h:14-20).
@@ -43,7 +47,7 @@ __device__ __forceinline__ double upd2_exact(double a, double b, double f, doubl
   const double ab = __dsub_rn(a, b);
   const double disc =
       __dsub_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, f), f), h), h), __dmul_rn(ab, ab));
-  return __ddiv_rn(__dadd_rn(__dadd_rn(a, b), __dsqrt_rn(disc)), 2.0);
+  return __dmul_rn(__dadd_rn(__dadd_rn(a, b), __dsqrt_rn(disc)), 0.5);
 }
 
 template <class T>

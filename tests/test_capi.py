@@ -115,17 +115,17 @@ def test_valid_call_without_gpu_reports_nodev():
 
 def test_eikonal3d_rejects_grids_deeper_than_the_brick_packing():
     """Brick coordinates are packed in 11/11/10 bits: more than 1023 bricks of
-    32 cells along k would wrap, so the plain 3D entry points reject such a
-    grid before any device work."""
+    16 cells (the plain path's brick depth) along k would wrap, so the plain 3D
+    entry points reject such a grid before any device work."""
     import ctypes as C
     L = A.lib()
     st = _lib.SolveStatus()
-    for l in (32 * 1023 + 1, 40000):
+    for l in (16 * 1023 + 1, 40000):
         assert L.adt_eikonal_three_d_device(None, None, 1.0, 2, 2, l, 1e-6, 0, None,
                                             C.byref(st), None) == -1
         assert b"too deep" in L.adt_last_error()
     # the deepest accepted grid passes the size checks (and fails on the null arrays)
-    assert L.adt_eikonal_three_d_device(None, None, 1.0, 2, 2, 32 * 1023, 1e-6, 0, None,
+    assert L.adt_eikonal_three_d_device(None, None, 1.0, 2, 2, 16 * 1023, 1e-6, 0, None,
                                         C.byref(st), None) == -1
     assert b"null array" in L.adt_last_error()
 
