@@ -282,7 +282,7 @@ def run_ours(args, rank, world):
     sf = np.zeros(N_EVENTS, np.int32)
     # observed times: FP64 on the +2% noise model, reference stopping rule (setup, untimed)
     t_obs = gpu_picks(A)
-    B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6, bk=args.bk,
+    B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=args.tol, bk=args.bk,
                   warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
                   adj_wake_tol=args.adj_wake_tol, fwd_order_filter=bool(args.fwd_order_filter),
                   adj_warps=args.adj_warps, adj_groups=args.adj_groups)
@@ -381,7 +381,7 @@ def run_ours(args, rank, world):
         # events, picks and options as the headline plan (untimed)
         k = cpu_sample
         E = A.Batch3D([(M, N, L, H)], [sta], np.zeros(k, np.int32), src[:k], precision=A.ADT_F32,
-                      tol=1e-6, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
+                      tol=args.tol, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
                       fwd_order_filter=bool(args.fwd_order_filter))
         mis_k, tp_k, (g_k,), _ = E.run([f], t_obs[:k * N_STA], w[:k * N_STA])
         E.close()
@@ -426,7 +426,7 @@ def run_ours(args, rank, world):
                    "ctas": st.ctas,
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
-                   "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
+                   "tol": args.tol, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
                    "fwd_order_filter": args.fwd_order_filter,
                    "picks": "FP64 travel times on the +2%-noise model (reference stopping rule)",
                    "vs_exact_skipping": vs_exact, "error_vs_fp64": err64},
@@ -774,6 +774,8 @@ def main():
                          "configurations; c4, c5: secondary lines for the larger "
                          "configurations; c5inv: C5's 10 L-BFGS iterations; inversion: the "
                          "inversion driver on the C3 grid, FP32 against FP64")
+    ap.add_argument("--tol", type=float, default=1e-6,
+                    help="forward stopping tolerance of the FP32 plan (s; default 1e-6)")
     ap.add_argument("--wake-tol", type=float, default=1e-6,
                     help="forward: a brick that moved by at most this (s) wakes no neighbour "
                          "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
