@@ -486,6 +486,39 @@ def test_batch_chunking_and_graph_do_not_change_results():
     ref_x.close()
 
 
+def test_batch_overlapping_chunks_uneven_fields():
+    """Two chunks resident on two streams (overlap_chunks) with solves on
+    fields of different size, ragged chunk counts and graph replay on and
+    off: the same bits as one chunk of all solves, FP32 and FP64; with the
+    reference stopping rule (one buffer set, overlap ignored) bit-exact to
+    the oracle."""
+    rng = np.random.default_rng(17)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(20, 18, 14, 0.5), (12, 26, 40, 0.25)], 9, 7)
+    for prec in (A.ADT_F32, A.ADT_F64):
+        R = A.Batch3D(fields, stations, sf, src, precision=prec, tol=1e-6)
+        r = R.run(slow, t_obs, w)
+        R.close()
+        for kw in ({"chunk": 2}, {"chunk": 4, "use_graph": False}, {"chunk": 5}):
+            B = A.Batch3D(fields, stations, sf, src, precision=prec, tol=1e-6, overlap_chunks=True,
+                          **kw)
+            for _ in range(2):  # replays reuse both buffer sets
+                out = B.run(slow, t_obs, w)
+                assert out[0] == r[0] and np.array_equal(out[1], r[1]), (prec, kw)
+                for a, b in zip(out[2], r[2]):
+                    assert np.array_equal(a, b), (prec, kw)
+            B.close()
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True,
+                  chunk=3, overlap_chunks=True)
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, ito = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-6, 20)
+    assert mis == mo and np.array_equal(tp, tpo)
+    for g, r_ in zip(grads, go):
+        assert np.array_equal(g, r_)
+    assert [x.iters for x in st] == list(ito)
+    B.close()
+
+
 def test_batch_nonconvergence_is_reported():
     rng = np.random.default_rng(10)
     fields, stations, slow, sf, src, t_obs, w = make_batch(rng, [(30, 30, 20, 0.5)], 2, 5)
