@@ -779,8 +779,8 @@ def main():
     ap.add_argument("--wake-tol", type=float, default=1e-6,
                     help="forward: a brick that moved by at most this (s) wakes no neighbour "
                          "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
-    ap.add_argument("--adj-wake-tol", type=float, default=1e-5,
-                    help="adjoint: the same for relative changes (default 1e-5; 0 = exact)")
+    ap.add_argument("--adj-wake-tol", type=float, default=1e-4,
+                    help="adjoint: the same for relative changes (default 1e-4; 0 = exact)")
     ap.add_argument("--fwd-order-filter", type=int, default=1,
                     help="1 (library default): FP32 forward sweeps each brick only in the "
                          "orderings that follow its learned upwind directions; 0: all")
