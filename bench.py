@@ -495,7 +495,8 @@ def run_large(args):
     fields, stations, slow, sf, src, chunk, desc = large_workload(args.workload, rng)
     B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, chunk=chunk,
                   wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
-                  overlap_chunks=bool(args.overlap_chunks))
+                  overlap_chunks=bool(args.overlap_chunks), warps=args.warps, groups=args.groups,
+                  adj_warps=args.adj_warps, adj_groups=args.adj_groups)
     n_obs = sum(len(stations[f]) for f in sf)
     B.upload(slow, np.full(n_obs, 1.0), np.ones(n_obs))
     B.run_resident()
@@ -523,6 +524,8 @@ def run_large(args):
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "solves": int(len(sf)), "chunk": chunk,
                    "overlap_chunks": args.overlap_chunks if chunk else 0,
+                   "shapes": {"warps": st.warps, "groups": st.groups, "adj_warps": st.adj_warps,
+                              "adj_groups": st.adj_groups},
                    "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
                    "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
                    "cell_updates_per_s": (st.fwd_cell_updates + st.adj_cell_updates) /
