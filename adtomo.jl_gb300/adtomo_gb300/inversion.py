@@ -160,11 +160,12 @@ class TravelTimeInversion:
     sizes; lambda_p = 0 disables it).  tol, max_iter: forward stopping rule
     (the script passes tol = 1e-3 to eikonal3d, whose cap is 20 iterations).
     The near-source initial values come from vel0 for the whole run, as in
-    the script (:52-60).
+    the script (:52-60).  autotune > 0 (FP32): time the plan's launch shapes
+    on the starting model with that many evaluations per candidate first.
     """
 
     def __init__(self, grid, vel0, stations, events, uobs, qua, lambda_p=0.0, smooth_hor=1,
-                 smooth_ver=1, tol=1e-3, max_iter=20, precision=ADT_F32, **plan_kw):
+                 smooth_ver=1, tol=1e-3, max_iter=20, precision=ADT_F32, autotune=0, **plan_kw):
         m, n, l, h = grid
         self.shape = (int(m), int(n), int(l))
         self.vel0 = _f64(vel0, "vel0").reshape(self.shape)
@@ -179,6 +180,10 @@ class TravelTimeInversion:
         self.plan = Batch3D([(m, n, l, h)], [self.events], np.zeros(S, np.int32), self.stations,
                             precision=precision, tol=tol, max_iter=max_iter, **plan_kw)
         self.plan.set_source_velocity([self.vel0])
+        if autotune and precision == ADT_F32:
+            # launch shapes timed on the starting model (adt_batch_autotune, `autotune` reps)
+            self.plan.upload([1.0 / self.vel0], self.uobs, self.qua)
+            self.plan.autotune(reps=int(autotune))
         self.evaluations = 0
         self.last_status = None
 

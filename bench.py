@@ -714,7 +714,8 @@ def run_c5_inversion(args):
 
     def invert(k_eve, iters, prec):
         inv = TravelTimeInversion((m, n, l, h), vel0, eve[:k_eve], sta, uobs[:k_eve], qua[:k_eve],
-                                  lambda_p=0.0, precision=prec, **opts)
+                                  lambda_p=0.0, precision=prec, autotune=1 if args.autotune else 0,
+                                  **opts)
         t1 = time.perf_counter()
         x, loss, hist = inv.optimize(iterations=iters)
         dt = time.perf_counter() - t1
