@@ -289,8 +289,9 @@ int batch_check_args(int32_t n_fields, const int32_t* dims, const double* hh, co
     return set_error(ADT_EINVAL, "batch: precision must be ADT_F32 or ADT_F64");
   if (o.ref_compat && o.precision != ADT_F64)
     return set_error(ADT_EINVAL, "batch: ref_compat needs ADT_F64");
-  if (o.max_iter < 1 || o.adj_max_iter < 1 || !(o.tol >= 0.0))
-    return set_error(ADT_EINVAL, "batch: bad iteration caps or tolerance");
+  if (o.max_iter < 1 || o.adj_max_iter < 1 || o.max_iter > 100000 || o.adj_max_iter > 100000 ||
+      !(o.tol >= 0.0))
+    return set_error(ADT_EINVAL, "batch: bad iteration caps (1..100000) or tolerance");
   if (!(o.wake_tol >= 0.0) || !std::isfinite(o.wake_tol) || !(o.adj_wake_tol >= 0.0) ||
       !std::isfinite(o.adj_wake_tol))
     return set_error(ADT_EINVAL, "batch: wake_tol and adj_wake_tol must be finite and >= 0");
@@ -332,6 +333,11 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   for (int f = 0; f < n_fields; ++f) {
     const Geom g = make_geom(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2], P->bk);
     if (g.nbz > 1023) return set_error(ADT_EINVAL, "batch: field %d is too deep", f);
+    // brick timestamps count level steps, (iteration * 8 + ordering) * levels + level,
+    // in an int
+    if ((int64_t)(std::max(P->opts.max_iter, o.adj_max_iter) + 1) * 8 * g.nlev >= INT_MAX)
+      return set_error(ADT_EINVAL, "batch: field %d has too many brick levels (%d) for the "
+                       "iteration caps", f, g.nlev);
     P->geoms.push_back(g);
     P->h.push_back(hh[f]);
     P->nsta.push_back(nsta[f]);

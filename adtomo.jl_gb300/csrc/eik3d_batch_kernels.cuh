@@ -283,7 +283,7 @@ __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx&
 // rank gw, gw + GW, ...: equal shares however the dirty bricks are spread,
 // without a barrier before the level; one named barrier after it.
 //
-// body(p) sweeps one dirty brick and returns whether it changed; this
+// body(p, fbits) sweeps one dirty brick and returns whether it changed; this
 // function keeps the brick's timestamps (t = ts0 + level) and counters.
 //
 // flow (adjoint only, else null): per brick, the directions in which adjoint
@@ -295,12 +295,13 @@ __device__ __forceinline__ int group_next(const BatchArgs<T>& A, const GroupCtx&
 //
 // fmask (FP32 forward only, else null): per brick, the upwind directions its
 // changing sweeps have seen, learned during the solve (FWD_FLOW_KNOWN set
-// once one has), with the level time of the last write in the bits above 8.
-// A dirty brick with a known mask is swept only in the orderings that follow
-// it.  The sweeper writes the entry while other warps may still be testing
-// the brick in the same level; an entry written at the current level time
-// reads as allowed, which is what the sweeper found before it swept, so all
-// warps still agree.  body(p, fbits) returns the sweep's upwind bits
+// once one has), with the level time of the last write (modulo 2^24) in the
+// bits above 8.  A dirty brick with a known mask is swept only in the
+// orderings that follow it.  The sweeper writes the entry while other warps
+// may still be testing the brick in the same level; an entry written at the
+// current level time reads as allowed, which is what the sweeper found before
+// it swept, so all warps still agree.  (An entry 2^24 level steps old also
+// reads as allowed: a spare sweep, never a missed one.)  body(p, fbits) returns the sweep's upwind bits
 // (absolute, as the adjoint's flow bits) in fbits.
 constexpr int FWD_FLOW_KNOWN = 0x80;
 
@@ -321,7 +322,8 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
     if (fmask) {
       const int e = ((const volatile int*)fmask)[b];
       return brick_dirty(mod, proc, g, b, bx, by, bz, t) &&
-             (!(e & FWD_FLOW_KNOWN) || (e >> 8) == t || adjoint_flow_allowed(e & 63, forbid));
+             (!(e & FWD_FLOW_KNOWN) || ((unsigned)e >> 8) == ((unsigned)t & 0xFFFFFFu) ||
+              adjoint_flow_allowed(e & 63, forbid));
     }
     return brick_dirty(mod, proc, g, b, bx, by, bz, t);
   };
@@ -401,8 +403,8 @@ __device__ __forceinline__ void run_ordering(const GroupCtx& c, const Geom& g, c
             }
             if (fmask && fbits) {
               const int old = fmask[b];
-              fmask[b] = (t << 8) | FWD_FLOW_KNOWN | ((old & FWD_FLOW_KNOWN) ? (old & 63) : 0) |
-                         (int)fbits;
+              fmask[b] = (int)((((unsigned)t & 0xFFFFFFu) << 8) | FWD_FLOW_KNOWN |
+                               ((old & FWD_FLOW_KNOWN) ? (old & 63) : 0) | fbits);
             }
             cnt_upd += (unsigned long long)p.ni * p.nj * p.nk;
             cnt_brk += 1;
