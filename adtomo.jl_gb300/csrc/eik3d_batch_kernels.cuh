@@ -771,27 +771,40 @@ __device__ __forceinline__ int upwind_side_t(const T* u, int64_t c, int pos, int
 // 16-byte loads: the same rule as upwind_side_t and the fixed-cell test,
 // with out-of-grid neighbours read as +inf (so the edge cases fall out of the
 // comparisons).  Writes the four codes (one 8-byte store) and lambda = 0.
-__device__ __forceinline__ void adj_pass1_vec4(const float* u, uint16_t* code, float* lam,
-                                               const SolveDev& sd, const Geom& g, int64_t x,
-                                               int i, int j, int k) {
+// Split into the loads (p1_load; u is read-only in the adjoint kernel, so
+// through the read-only path) and the rest (p1_store), so that a caller can
+// issue the loads of several groups of cells before it waits for any.
+struct P1Loads {
+  float4 c4, xm, xp, ym, yp;
+  float zm, zp;
+};
+
+__device__ __forceinline__ P1Loads p1_load(const float* __restrict__ u, const Geom& g, int64_t x,
+                                           int i, int j, int k) {
   const float INF = __int_as_float(0x7f800000);
   const float4 INF4 = make_float4(INF, INF, INF, INF);
   const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
-  const float4 c4 = *reinterpret_cast<const float4*>(u + x);
-  const float4 xm = i > 0 ? *reinterpret_cast<const float4*>(u + x - sI) : INF4;
-  const float4 xp = i < g.m - 1 ? *reinterpret_cast<const float4*>(u + x + sI) : INF4;
-  const float4 ym = j > 0 ? *reinterpret_cast<const float4*>(u + x - sJ) : INF4;
-  const float4 yp = j < g.n - 1 ? *reinterpret_cast<const float4*>(u + x + sJ) : INF4;
-  const float zm = k > 0 ? u[x - 1] : INF;
-  const float zp = k + 4 < g.l ? u[x + 4] : INF;
-  const float uc[4] = {c4.x, c4.y, c4.z, c4.w};
-  const float vxm[4] = {xm.x, xm.y, xm.z, xm.w}, vxp[4] = {xp.x, xp.y, xp.z, xp.w};
-  const float vym[4] = {ym.x, ym.y, ym.z, ym.w}, vyp[4] = {yp.x, yp.y, yp.z, yp.w};
+  P1Loads r;
+  r.c4 = __ldg(reinterpret_cast<const float4*>(u + x));
+  r.xm = i > 0 ? __ldg(reinterpret_cast<const float4*>(u + x - sI)) : INF4;
+  r.xp = i < g.m - 1 ? __ldg(reinterpret_cast<const float4*>(u + x + sI)) : INF4;
+  r.ym = j > 0 ? __ldg(reinterpret_cast<const float4*>(u + x - sJ)) : INF4;
+  r.yp = j < g.n - 1 ? __ldg(reinterpret_cast<const float4*>(u + x + sJ)) : INF4;
+  r.zm = k > 0 ? __ldg(u + x - 1) : INF;
+  r.zp = k + 4 < g.l ? __ldg(u + x + 4) : INF;
+  return r;
+}
+
+__device__ __forceinline__ void p1_store(const P1Loads& r, uint16_t* code, float* lam,
+                                         const SolveDev& sd, int64_t x, int i, int j, int k) {
+  const float uc[4] = {r.c4.x, r.c4.y, r.c4.z, r.c4.w};
+  const float vxm[4] = {r.xm.x, r.xm.y, r.xm.z, r.xm.w}, vxp[4] = {r.xp.x, r.xp.y, r.xp.z, r.xp.w};
+  const float vym[4] = {r.ym.x, r.ym.y, r.ym.z, r.ym.w}, vyp[4] = {r.yp.x, r.yp.y, r.yp.z, r.yp.w};
   uint32_t packed[2] = {0u, 0u};
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const float um[3] = {vxm[q], vym[q], q == 0 ? zm : uc[q - 1]};
-    const float up[3] = {vxp[q], vyp[q], q == 3 ? zp : uc[q + 1]};
+    const float um[3] = {vxm[q], vym[q], q == 0 ? r.zm : uc[q - 1]};
+    const float up[3] = {vxp[q], vyp[q], q == 3 ? r.zp : uc[q + 1]};
     uint32_t cd = 0;
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {  // upwind side: the smaller neighbour, ties to +1
@@ -808,22 +821,34 @@ __device__ __forceinline__ void adj_pass1_vec4(const float* u, uint16_t* code, f
 
 // User bits of four consecutive cells (pass 2) from 8-byte loads of the
 // codes: neighbour r uses c when r is not fixed and its upwind side along
-// the axis points at c.  Returns the OR of the four cells' user bits.
-__device__ __forceinline__ uint32_t adj_pass2_vec4(uint16_t* code, const Geom& g, int64_t x,
-                                                   int i, int j, int k) {
+// the axis points at c.  p2_load / p2_store split as in pass 1; the codes are
+// read through the ordinary path (pass 2 rewrites their user bits, never the
+// bits read here).  p2_store returns the OR of the four cells' user bits.
+struct P2Loads {
+  uint2 c4, xm, xp, ym, yp;
+  uint32_t zm, zp;
+};
+
+__device__ __forceinline__ P2Loads p2_load(const uint16_t* code, const Geom& g, int64_t x, int i,
+                                           int j, int k) {
   const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
   auto ld4 = [&](int64_t y) -> uint2 { return *reinterpret_cast<const uint2*>(code + y); };
+  const uint2 fixed4 = make_uint2(CODE_FIXED | (CODE_FIXED << 16), CODE_FIXED | (CODE_FIXED << 16));
+  P2Loads r;
+  r.c4 = ld4(x);
+  r.xm = i > 0 ? ld4(x - sI) : fixed4;
+  r.xp = i < g.m - 1 ? ld4(x + sI) : fixed4;
+  r.ym = j > 0 ? ld4(x - sJ) : fixed4;
+  r.yp = j < g.n - 1 ? ld4(x + sJ) : fixed4;
+  r.zm = k > 0 ? (uint32_t)code[x - 1] : CODE_FIXED;
+  r.zp = k + 4 < g.l ? (uint32_t)code[x + 4] : CODE_FIXED;
+  return r;
+}
+
+__device__ __forceinline__ uint32_t p2_store(const P2Loads& r, uint16_t* code, int64_t x) {
   auto c16 = [](uint2 v, int q) -> uint32_t {
     return ((q < 2 ? v.x : v.y) >> (16 * (q & 1))) & 0xffffu;
   };
-  const uint2 zero = make_uint2(CODE_FIXED | (CODE_FIXED << 16), CODE_FIXED | (CODE_FIXED << 16));
-  const uint2 c4 = ld4(x);
-  const uint2 xm = i > 0 ? ld4(x - sI) : zero;
-  const uint2 xp = i < g.m - 1 ? ld4(x + sI) : zero;
-  const uint2 ym = j > 0 ? ld4(x - sJ) : zero;
-  const uint2 yp = j < g.n - 1 ? ld4(x + sJ) : zero;
-  const uint32_t zm = k > 0 ? (uint32_t)code[x - 1] : CODE_FIXED;
-  const uint32_t zp = k + 4 < g.l ? (uint32_t)code[x + 4] : CODE_FIXED;
   auto uses = [](uint32_t cr, int ax, uint32_t want) -> bool {
     return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
   };
@@ -831,15 +856,15 @@ __device__ __forceinline__ uint32_t adj_pass2_vec4(uint16_t* code, const Geom& g
   uint32_t all = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    uint32_t cd = c16(c4, q);
+    uint32_t cd = c16(r.c4, q);
     if (!(cd & CODE_FIXED)) {
       uint32_t us = 0;
-      if (uses(c16(xm, q), 0, 2u)) us |= 1u;
-      if (uses(c16(xp, q), 0, 1u)) us |= 2u;
-      if (uses(c16(ym, q), 1, 2u)) us |= 4u;
-      if (uses(c16(yp, q), 1, 1u)) us |= 8u;
-      if (uses(q == 0 ? zm : c16(c4, q - 1), 2, 2u)) us |= 16u;
-      if (uses(q == 3 ? zp : c16(c4, q + 1), 2, 1u)) us |= 32u;
+      if (uses(c16(r.xm, q), 0, 2u)) us |= 1u;
+      if (uses(c16(r.xp, q), 0, 1u)) us |= 2u;
+      if (uses(c16(r.ym, q), 1, 2u)) us |= 4u;
+      if (uses(c16(r.yp, q), 1, 1u)) us |= 8u;
+      if (uses(q == 0 ? r.zm : c16(r.c4, q - 1), 2, 2u)) us |= 16u;
+      if (uses(q == 3 ? r.zp : c16(r.c4, q + 1), 2, 1u)) us |= 32u;
       cd |= us << CODE_USERS;
       all |= us;
     }
@@ -903,11 +928,19 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     // pass 1: upwind sides and fixed cells; lambda = 0
     const bool vec4 = sizeof(T) == 4 && (g.l % 4) == 0;
     if constexpr (sizeof(T) == 4) {
+      // two groups of four cells per step, all their loads issued first
       if (vec4)
-        for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += c.gthreads) {
-          const int64_t col = e / (g.l / 4);
-          adj_pass1_vec4(u, code, lam, sd, g, 4 * e, (int)(col / g.n), (int)(col % g.n),
-                         (int)(4 * e - col * g.l));
+        for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += 2 * c.gthreads) {
+          const int64_t e2 = e + c.gthreads;
+          const bool two = e2 < g.ncell / 4;
+          const int64_t col = e / (g.l / 4), col2 = (two ? e2 : e) / (g.l / 4);
+          const int i = (int)(col / g.n), j = (int)(col % g.n), k = (int)(4 * e - col * g.l);
+          const int i2 = (int)(col2 / g.n), j2 = (int)(col2 % g.n);
+          const int k2 = (int)(4 * (two ? e2 : e) - col2 * g.l);
+          const P1Loads a = p1_load(u, g, 4 * e, i, j, k);
+          const P1Loads b = p1_load(u, g, 4 * (two ? e2 : e), i2, j2, k2);
+          p1_store(a, code, lam, sd, 4 * e, i, j, k);
+          if (two) p1_store(b, code, lam, sd, 4 * e2, i2, j2, k2);
         }
     }
     for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
@@ -940,10 +973,17 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
     };
     if constexpr (sizeof(T) == 4) {
       if (vec4)
-        for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += c.gthreads) {
-          const int64_t col = e / (g.l / 4);
+        for (int64_t e = c.gw * 32 + lane; e < g.ncell / 4; e += 2 * c.gthreads) {
+          const int64_t e2 = e + c.gthreads;
+          const bool two = e2 < g.ncell / 4;
+          const int64_t col = e / (g.l / 4), col2 = (two ? e2 : e) / (g.l / 4);
           const int i = (int)(col / g.n), j = (int)(col % g.n), k = (int)(4 * e - col * g.l);
-          add_flow(i, j, k, adj_pass2_vec4(code, g, 4 * e, i, j, k));
+          const int i2 = (int)(col2 / g.n), j2 = (int)(col2 % g.n);
+          const int k2 = (int)(4 * (two ? e2 : e) - col2 * g.l);
+          const P2Loads a = p2_load(code, g, 4 * e, i, j, k);
+          const P2Loads b = p2_load(code, g, 4 * (two ? e2 : e), i2, j2, k2);
+          add_flow(i, j, k, p2_store(a, code, 4 * e));
+          if (two) add_flow(i2, j2, k2, p2_store(b, code, 4 * e2));
         }
     }
     for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
