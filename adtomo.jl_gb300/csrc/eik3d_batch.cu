@@ -751,8 +751,8 @@ int batch_autotune(BatchPlan* P, int reps) {
   if ((P->uploaded & 7) != 7)
     return set_error(ADT_EINVAL, "batch: upload slowness, t_obs and weight before autotune");
   reps = std::max(1, std::min(reps, 16));
-  const int fwd_c[] = {3, 4, 5, 6, 8, 12};
-  const int adj_c[] = {2, 3, 4, 6, 8};
+  const int fwd_c[] = {3, 4, 5, 6, 8, 10, 12};
+  const int adj_c[] = {2, 3, 4, 6, 7, 8, 9};
   auto measure = [&](float& fwd_ms, float& adj_ms) -> int {
     fwd_ms = adj_ms = 1e30f;
     for (int r = 0; r < reps; ++r) {
