@@ -21,6 +21,7 @@ ERRORS = {
     -7: "ADT_ENODEV",
 }
 ADT_F32, ADT_F64 = 0, 1
+ADT_ADJ_SWEEPS, ADT_ADJ_CAUSAL = 0, 1
 
 
 class AdtError(RuntimeError):
@@ -45,7 +46,7 @@ class BatchOpts(C.Structure):
                 ("wake_tol", C.c_double), ("adj_wake_tol", C.c_double),
                 ("adj_order_filter", C.c_int32), ("fwd_order_filter", C.c_int32),
                 ("overlap_chunks", C.c_int32), ("adj_warps", C.c_int32),
-                ("adj_groups", C.c_int32)]
+                ("adj_groups", C.c_int32), ("adj_solver", C.c_int32)]
 
 
 class BatchStats(C.Structure):

@@ -14,7 +14,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import ADT_F32, ADT_F64, AdtError, BatchOpts, BatchStats, SolveStatus, check, lib
+from ._lib import (ADT_ADJ_CAUSAL, ADT_ADJ_SWEEPS, ADT_F32, ADT_F64, AdtError, BatchOpts,
+                   BatchStats, SolveStatus, check, lib)
 
 __all__ = ["eikonal", "eikonal_grad", "eikonal_batch", "eikonal3d", "eikonal3d_grad", "Batch3D",
            "AdtError", "ADT_F32", "ADT_F64"]
@@ -124,14 +125,16 @@ class Batch3D:
     Options are the fields of adt_batch_opts (include/adtomo_gpu.h); in
     particular wake_tol / adj_wake_tol (FP32 only, default 0 = exact brick
     skipping) let bricks that moved by at most that much (seconds; relative
-    for the adjoint) leave their neighbours asleep.
+    for the adjoint) leave their neighbours asleep.  adj_solver "causal"
+    (ADT_ADJ_CAUSAL) solves each adjoint system once in reverse causal order
+    instead of by sweeps ("sweeps", ADT_ADJ_SWEEPS).
     """
 
     def __init__(self, fields, stations, solve_field, src_xyz, precision=ADT_F32, tol=1e-6,
                  max_iter=200, adj_max_iter=200, ref_compat=False, near_src_f64=2, chunk=0,
                  bk=0, warps=0, groups=0, use_graph=True, wake_tol=0.0, adj_wake_tol=0.0,
                  adj_order_filter=True, fwd_order_filter=True, overlap_chunks=False,
-                 adj_warps=0, adj_groups=0):
+                 adj_warps=0, adj_groups=0, adj_solver="sweeps"):
         L = lib()
         self._L = L
         self.fields = [tuple(x) for x in fields]
@@ -155,6 +158,8 @@ class Batch3D:
         o.fwd_order_filter = int(bool(fwd_order_filter))
         o.overlap_chunks = int(bool(overlap_chunks))
         o.adj_warps, o.adj_groups = adj_warps, adj_groups
+        solvers = {"sweeps": ADT_ADJ_SWEEPS, "causal": ADT_ADJ_CAUSAL}
+        o.adj_solver = solvers[adj_solver] if isinstance(adj_solver, str) else int(adj_solver)
         self._keep = (dims, hs, sta, src)
         h = C.c_void_p()
         check(L.adt_batch_create(C.byref(h), len(self.fields), _ptr(dims), _ptr(hs),

@@ -91,6 +91,9 @@ __host__ __device__ __forceinline__ void ordering3(int o, int& si, int& sj, int&
 constexpr uint16_t CODE_FIXED = 1u << 6;
 constexpr uint16_t CODE_SEED = 1u << 7;
 constexpr int CODE_USERS = 8;
+// Outstanding-user byte of a fixed cell in the causal-order adjoint: never
+// cleared by a user, so the cell is never queued.
+constexpr uint32_t REM_FIXED = 0x80u;
 
 // Geometry of one field as seen by the kernels.
 struct Geom {

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "eik3d_batch.h"
+#include "eik3d_adj_causal.cuh"
 #include "eik3d_batch_kernels.cuh"
 #include "eik3d_common_host.h"
 
@@ -86,15 +87,27 @@ size_t adj_warp_smem(int bk) {
   return 2 * (size_t)te * sizeof(T) + (size_t)ie * sizeof(uint16_t);
 }
 
+// Multipliers of the causal-order adjoint's cell-index divisions (FieldDev).
+template <class T>
+void set_divisors(FieldDev<T>& fd) {
+  const unsigned long long nl = (unsigned long long)fd.g.n * fd.g.l, l = fd.g.l;  // both >= 2
+  fd.div_nl = ~0ULL / nl + 1;
+  fd.div_l = ~0ULL / l + 1;
+}
+
 }  // namespace
 
 // Kernel entry points per (T, BK), resolved at plan creation.
 struct KernelSet {
   const void* fwd;
   const void* adj;
+  const void* adj_causal;
   const void* misfit;
   const void* grad;
 };
+
+// Queue entries per thread per pass of the causal-order adjoint.
+constexpr int CAUSAL_NB = 2;
 
 template <class T>
 static KernelSet kernels_for(int bk) {
@@ -110,6 +123,7 @@ static KernelSet kernels_for(int bk) {
     k.fwd = (const void*)&k_batch_fwd<T, 32, MODE>;
     k.adj = (const void*)&k_batch_adj<T, 32>;
   }
+  k.adj_causal = (const void*)&k_batch_adj_causal<T, CAUSAL_NB>;
   k.misfit = (const void*)&k_batch_misfit<T>;
   k.grad = (const void*)&k_batch_grad<T>;
   return k;
@@ -156,6 +170,7 @@ struct BatchPlan {
     DevBuf u, lam, code, meta, sidx, sval;
     DevBuf gdense;       // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
     DevBuf mis_scratch;  // seed merge arrays when they exceed shared memory
+    DevBuf rem, queue;   // causal-order adjoint: outstanding-user bytes and frontiers
   };
   ChunkBufs cb[2];
   int nsets = 1;
@@ -171,8 +186,9 @@ struct BatchPlan {
   KernelSet ks;
   int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
   int fwd_gw = 4, fwd_groups = 2, adj_gw = 2, adj_groups = 4;
+  bool causal = false;  // adjoint in causal order (k_batch_adj_causal, one solve per CTA)
   int max_nb = 0, meta_smem = 0;
-  int sm_count = 0, fwd_regs = 0, adj_regs = 0;
+  int sm_count = 0, fwd_regs = 0, adj_regs = 0, adj_maxt = 1024;
   size_t smem_budget = 0, fwd_wbytes = 0, adj_wbytes = 0;
   size_t fwd_smem = 0, adj_smem = 0, mis_smem = 0;
   // graph and timing
@@ -208,6 +224,7 @@ void batch_opts_default(adt_batch_opts* o) {
   o->overlap_chunks = 0;
   o->adj_warps = 0;
   o->adj_groups = 0;
+  o->adj_solver = ADT_ADJ_SWEEPS;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -257,10 +274,16 @@ static int apply_shapes(BatchPlan* P, int fwd_gw, int fwd_groups, int adj_gw, in
                       META_ARRAYS_FWD, P->smem_budget, fwd_gw > 0 ? fwd_gw : (P->f64 ? 2 : 6), fwd_groups,
                       P->fwd_gw, P->fwd_groups, P->fwd_smem)))
     return rc;
-  if ((rc = fit_shape(P->ks.adj, P->adj_wbytes, P->adj_regs, 1024, P->meta_smem, P->max_nb,
-                      META_ARRAYS_ADJ, P->smem_budget, adj_gw > 0 ? adj_gw : (P->f64 ? 2 : 4), adj_groups,
-                      P->adj_gw, P->adj_groups, P->adj_smem)))
+  if (P->causal) {  // one solve per CTA of adj_gw warps, static shared memory only
+    const int max_warps = std::min(P->adj_maxt / 32, 65536 / std::max(1, P->adj_regs * 32));
+    P->adj_gw = std::max(1, std::min(adj_gw > 0 ? adj_gw : 16, max_warps));
+    P->adj_groups = 1;
+    P->adj_smem = 0;
+  } else if ((rc = fit_shape(P->ks.adj, P->adj_wbytes, P->adj_regs, 1024, P->meta_smem, P->max_nb,
+                             META_ARRAYS_ADJ, P->smem_budget, adj_gw > 0 ? adj_gw : (P->f64 ? 2 : 4),
+                             adj_groups, P->adj_gw, P->adj_groups, P->adj_smem))) {
     return rc;
+  }
   P->fwd_warps = P->fwd_gw * P->fwd_groups;
   P->adj_warps = P->adj_gw * P->adj_groups;
   int occ_f = 0, occ_a = 0;
@@ -297,6 +320,8 @@ int batch_check_args(int32_t n_fields, const int32_t* dims, const double* hh, co
     return set_error(ADT_EINVAL, "batch: wake_tol and adj_wake_tol must be finite and >= 0");
   if (o.bk != 0 && o.bk != 16 && o.bk != 32 && o.bk != 64)
     return set_error(ADT_EINVAL, "batch: bk must be 0, 16, 32 or 64");
+  if (o.adj_solver != ADT_ADJ_SWEEPS && o.adj_solver != ADT_ADJ_CAUSAL)
+    return set_error(ADT_EINVAL, "batch: adj_solver must be ADT_ADJ_SWEEPS or ADT_ADJ_CAUSAL");
   return ADT_OK;
 }
 
@@ -329,6 +354,12 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   (void)minl;
   P->bk = o.bk ? o.bk : 32;
   P->nf = n_fields;
+  P->causal = o.adj_solver == ADT_ADJ_CAUSAL;
+  if (P->causal)
+    for (int f = 0; f < n_fields; ++f)
+      if ((int64_t)dims[3 * f] * dims[3 * f + 1] * dims[3 * f + 2] >= ((int64_t)1 << 31))
+        return set_error(ADT_EINVAL, "batch: the causal-order adjoint needs fewer than 2^31 cells "
+                         "per field (field %d)", f);
   int64_t sofs = 0;
   for (int f = 0; f < n_fields; ++f) {
     const Geom g = make_geom(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2], P->bk);
@@ -459,6 +490,10 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       R_(B.gdense, (size_t)max_cells * es);
       ADT_CUDA(cudaMemset(B.gdense.p, 0, (size_t)max_cells * es));
     }
+    if (P->causal) {
+      R_(B.rem, (size_t)max_cells);
+      R_(B.queue, (size_t)max_cells * 4);
+    }
   }
   if (P->nsets == 2) {
     ADT_CUDA(cudaStreamCreateWithFlags(&P->stream2, cudaStreamNonBlocking));
@@ -497,10 +532,12 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
       fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
       fdv[f].nsta = P->nsta[f];
+      set_divisors(fdv[f]);
     }
     R_(P->d_fields, n_fields * sizeof(FieldDev<double>));
     ADT_CUDA(cudaMemcpy(P->d_fields.p, fdv.data(), n_fields * sizeof(FieldDev<double>), cudaMemcpyHostToDevice));
     P->ks = kernels_for<double>(P->bk);
+    if (P->causal) P->ks.adj = P->ks.adj_causal;
   } else {
     std::vector<FieldDev<float>> fdv(n_fields);
     for (int f = 0; f < n_fields; ++f) {
@@ -513,10 +550,12 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
       fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
       fdv[f].nsta = P->nsta[f];
+      set_divisors(fdv[f]);
     }
     R_(P->d_fields, n_fields * sizeof(FieldDev<float>));
     ADT_CUDA(cudaMemcpy(P->d_fields.p, fdv.data(), n_fields * sizeof(FieldDev<float>), cudaMemcpyHostToDevice));
     P->ks = kernels_for<float>(P->bk);
+    if (P->causal) P->ks.adj = P->ks.adj_causal;
   }
   ADT_CUDA(cudaMemcpy(P->d_solves.p, P->solves.data(), n_solves * sizeof(SolveDev), cudaMemcpyHostToDevice));
   {
@@ -558,9 +597,11 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
     P->fwd_regs = fa_f.numRegs;
     P->adj_regs = fa_a.numRegs;
+    P->adj_maxt = fa_a.maxThreadsPerBlock;
   }
-  if ((rc = apply_shapes(P.get(), o.warps, o.groups, o.adj_warps ? o.adj_warps : o.warps,
-                          o.adj_groups ? o.adj_groups : o.groups)))
+  // the causal-order adjoint's width is warps per CTA, not a sweep group's
+  const int adj_w0 = o.adj_warps ? o.adj_warps : (P->causal ? 0 : o.warps);
+  if ((rc = apply_shapes(P.get(), o.warps, o.groups, adj_w0, o.adj_groups ? o.adj_groups : o.groups)))
     return rc;
   int maxsta = 0;
   for (int f = 0; f < n_fields; ++f) maxsta = std::max(maxsta, P->nsta[f]);
@@ -625,6 +666,8 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.max_nb = P.max_nb;
   A.adj_order_filter = P.opts.adj_order_filter ? 1 : 0;
   A.fwd_order_filter = (!P.f64 && P.opts.fwd_order_filter) ? 1 : 0;
+  A.rem = P.causal ? CB.rem.as<uint32_t>() : nullptr;
+  A.queue = P.causal ? CB.queue.as<int>() : nullptr;
   return A;
 }
 
@@ -752,7 +795,10 @@ int batch_autotune(BatchPlan* P, int reps) {
     return set_error(ADT_EINVAL, "batch: upload slowness, t_obs and weight before autotune");
   reps = std::max(1, std::min(reps, 16));
   const int fwd_c[] = {3, 4, 5, 6, 8, 10, 12};
-  const int adj_c[] = {2, 3, 4, 6, 7, 8, 9};
+  const int adj_sweeps[] = {2, 3, 4, 6, 7, 8, 9};
+  const int adj_causal[] = {4, 8, 12, 16, 24, 32};  // warps per CTA
+  const int* adj_c = P->causal ? adj_causal : adj_sweeps;
+  const int n_adj = P->causal ? 6 : 7;
   auto measure = [&](float& fwd_ms, float& adj_ms) -> int {
     fwd_ms = adj_ms = 1e30f;
     for (int r = 0; r < reps; ++r) {
@@ -777,7 +823,8 @@ int batch_autotune(BatchPlan* P, int reps) {
       best_f = gw;
     }
   }
-  for (int gw : adj_c) {
+  for (int t = 0; t < n_adj; ++t) {
+    const int gw = adj_c[t];
     if ((rc = apply_shapes(P, best_f, 0, gw, 0))) return rc;
     if (P->adj_gw != gw) continue;
     if ((rc = measure(ft, at))) return rc;

@@ -39,6 +39,10 @@ struct FieldDev {
   const int* lstart;        // nlev + 1
   const double* sta;        // receivers, 3 per station
   int nsta;
+  // floor(2^64 / d) + 1 for d = n * l and d = l: x / d = __umul64hi(x, .) for
+  // every 32-bit x (division by an invariant integer by multiplication; the
+  // error term x (d M - 2^64) / (d 2^64) stays below 1 / d when x < 2^32)
+  unsigned long long div_nl, div_l;
 };
 
 struct SolveDev {
@@ -86,6 +90,8 @@ struct BatchArgs {
   int adj_order_filter;     // 1: adjoint sweeps a brick only in the orderings its flow allows
   int fwd_order_filter;     // 1: FP32 forward sweeps a brick only in the orderings its
                             //    learned upwind directions allow
+  uint32_t* rem;            // causal-order adjoint: outstanding-user bytes, one per chunk cell
+  int* queue;               // causal-order adjoint: frontiers, one int per chunk cell
 };
 
 // Per-group scalars at the start of dynamic shared memory.
@@ -823,7 +829,9 @@ __device__ __forceinline__ void p1_store(const P1Loads& r, uint16_t* code, float
 // codes: neighbour r uses c when r is not fixed and its upwind side along
 // the axis points at c.  p2_load / p2_store split as in pass 1; the codes are
 // read through the ordinary path (pass 2 rewrites their user bits, never the
-// bits read here).  p2_store returns the OR of the four cells' user bits.
+// bits read here).  p2_store returns one byte per cell (cell q in bits
+// 8q..8q+7): its user bits, or REM_FIXED for a fixed cell (the outstanding-
+// user bytes of the causal-order adjoint, and the flow bits of the sweeps).
 struct P2Loads {
   uint2 c4, xm, xp, ym, yp;
   uint32_t zm, zp;
@@ -853,11 +861,13 @@ __device__ __forceinline__ uint32_t p2_store(const P2Loads& r, uint16_t* code, i
     return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
   };
   uint32_t packed[2] = {0u, 0u};
-  uint32_t all = 0;
+  uint32_t bytes = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     uint32_t cd = c16(r.c4, q);
-    if (!(cd & CODE_FIXED)) {
+    if (cd & CODE_FIXED) {
+      bytes |= (uint32_t)REM_FIXED << (8 * q);
+    } else {
       uint32_t us = 0;
       if (uses(c16(r.xm, q), 0, 2u)) us |= 1u;
       if (uses(c16(r.xp, q), 0, 1u)) us |= 2u;
@@ -866,12 +876,17 @@ __device__ __forceinline__ uint32_t p2_store(const P2Loads& r, uint16_t* code, i
       if (uses(q == 0 ? r.zm : c16(r.c4, q - 1), 2, 2u)) us |= 16u;
       if (uses(q == 3 ? r.zp : c16(r.c4, q + 1), 2, 1u)) us |= 32u;
       cd |= us << CODE_USERS;
-      all |= us;
+      bytes |= us << (8 * q);
     }
     packed[q >> 1] |= cd << (16 * (q & 1));
   }
   *reinterpret_cast<uint2*>(code + x) = make_uint2(packed[0], packed[1]);
-  return all;
+  return bytes;
+}
+
+// OR of the user bits in a word of four p2_store bytes.
+__device__ __forceinline__ uint32_t users_of4(uint32_t bytes) {
+  return (bytes | (bytes >> 8) | (bytes >> 16) | (bytes >> 24)) & 0x3fu;
 }
 
 template <int BK>
@@ -982,8 +997,8 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
           const int k2 = (int)(4 * (two ? e2 : e) - col2 * g.l);
           const P2Loads a = p2_load(code, g, 4 * e, i, j, k);
           const P2Loads b = p2_load(code, g, 4 * (two ? e2 : e), i2, j2, k2);
-          add_flow(i, j, k, p2_store(a, code, 4 * e));
-          if (two) add_flow(i2, j2, k2, p2_store(b, code, 4 * e2));
+          add_flow(i, j, k, users_of4(p2_store(a, code, 4 * e)));
+          if (two) add_flow(i2, j2, k2, users_of4(p2_store(b, code, 4 * e2)));
         }
     }
     for (int64_t col = vec4 ? (int64_t)g.m * g.n : c.gw; col < (int64_t)g.m * g.n; col += c.GW) {

@@ -215,14 +215,14 @@ def gpu_picks(A):
     return tp
 
 
-def fp64_batched_events_per_s(A, t_obs, steps=1):
-    """The same batched plan in FP64 (exact brick skipping, tol 1e-6): the
-    yardstick the FP32 path is measured against.  CUDA events around `steps`
-    evaluations after one warm-up."""
+def fp64_batched_events_per_s(A, t_obs, steps=1, adj_solver="sweeps"):
+    """The same batched plan in FP64 (exact brick skipping, tol 1e-6, the same
+    adjoint solver): the yardstick the FP32 path is measured against.  CUDA
+    events around `steps` evaluations after one warm-up."""
     import torch
     f, f_obs, sta, src, w = workload()
     P = A.Batch3D([(M, N, L, H)], [sta], np.zeros(N_EVENTS, np.int32), src, precision=A.ADT_F64,
-                  tol=1e-6)
+                  tol=1e-6, adj_solver=adj_solver)
     P.upload([f], t_obs, w)
     P.run_resident()
     torch.cuda.synchronize()
@@ -285,7 +285,8 @@ def run_ours(args, rank, world):
     B = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=args.tol, bk=args.bk,
                   warps=args.warps, groups=args.groups, wake_tol=args.wake_tol,
                   adj_wake_tol=args.adj_wake_tol, fwd_order_filter=bool(args.fwd_order_filter),
-                  adj_warps=args.adj_warps, adj_groups=args.adj_groups)
+                  adj_warps=args.adj_warps, adj_groups=args.adj_groups,
+                  adj_solver=args.adj_solver)
     B.upload([f], t_obs, w)
     if args.autotune and not (args.warps or args.groups or args.adj_warps or args.adj_groups):
         B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
@@ -382,7 +383,7 @@ def run_ours(args, rank, world):
         k = cpu_sample
         E = A.Batch3D([(M, N, L, H)], [sta], np.zeros(k, np.int32), src[:k], precision=A.ADT_F32,
                       tol=args.tol, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
-                      fwd_order_filter=bool(args.fwd_order_filter))
+                      fwd_order_filter=bool(args.fwd_order_filter), adj_solver=args.adj_solver)
         mis_k, tp_k, (g_k,), _ = E.run([f], t_obs[:k * N_STA], w[:k * N_STA])
         E.close()
         mo, tpo, go = cpu_out
@@ -401,7 +402,7 @@ def run_ours(args, rank, world):
                            if args.plain_sample > 0 else (None, 0.0))
     f64b = None
     if args.fp64_batched:
-        v64, ms64, st64 = fp64_batched_events_per_s(A, t_obs)
+        v64, ms64, st64 = fp64_batched_events_per_s(A, t_obs, adj_solver=args.adj_solver)
         f64b = {"value": v64, "unit": "events/s", "ms_per_evaluation": ms64,
                 "fwd_ms": st64.fwd_ms, "adj_ms": st64.adj_ms,
                 "cell_updates": int(st64.fwd_cell_updates + st64.adj_cell_updates),
@@ -427,7 +428,7 @@ def run_ours(args, rank, world):
                    "fwd_iters_mean": float(np.mean(iters)),
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
                    "tol": args.tol, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
-                   "fwd_order_filter": args.fwd_order_filter,
+                   "fwd_order_filter": args.fwd_order_filter, "adj_solver": args.adj_solver,
                    "picks": "FP64 travel times on the +2%-noise model (reference stopping rule)",
                    "vs_exact_skipping": vs_exact, "error_vs_fp64": err64},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
@@ -496,7 +497,8 @@ def run_large(args):
     B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, chunk=chunk,
                   wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
                   overlap_chunks=bool(args.overlap_chunks), warps=args.warps, groups=args.groups,
-                  adj_warps=args.adj_warps, adj_groups=args.adj_groups)
+                  adj_warps=args.adj_warps, adj_groups=args.adj_groups,
+                  adj_solver=args.adj_solver)
     n_obs = sum(len(stations[f]) for f in sf)
     B.upload(slow, np.full(n_obs, 1.0), np.ones(n_obs))
     B.run_resident()
@@ -527,7 +529,7 @@ def run_large(args):
                    "shapes": {"warps": st.warps, "groups": st.groups, "adj_warps": st.adj_warps,
                               "adj_groups": st.adj_groups},
                    "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
-                   "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
+                   "adj_solver": args.adj_solver, "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
                    "cell_updates_per_s": (st.fwd_cell_updates + st.adj_cell_updates) /
                    (ms_step / 1000.0),
                    "fwd_iters_mean": float(np.mean([x.iters for x in status])),
@@ -702,7 +704,7 @@ def run_c5_inversion(args):
     sta = synth.surface_stations(m, n, n_sta, rng)
     eve = synth.volume_sources(m, n, l, n_eve, rng)
     opts = dict(tol=1e-6, max_iter=200, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
-                chunk=chunk, overlap_chunks=bool(args.overlap_chunks))
+                chunk=chunk, overlap_chunks=bool(args.overlap_chunks), adj_solver=args.adj_solver)
     t0 = time.perf_counter()
     P = A.Batch3D([(m, n, l, h)], [sta], np.zeros(n_eve, np.int32), eve, precision=A.ADT_F32,
                   **opts)
@@ -741,7 +743,8 @@ def run_c5_inversion(args):
                    "seconds_total": full["s"], "picks_setup_s": picks_s,
                    "loss_history": full["hist"],
                    "model_error_rel": float(np.linalg.norm(full["v"] - v_true) / err0),
-                   "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol},
+                   "tol": 1e-6, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
+                   "adj_solver": args.adj_solver},
     }
     if r64 is not None:
         dv64 = np.linalg.norm(r64["v"] - vel0)
@@ -785,6 +788,9 @@ def main():
                          "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
     ap.add_argument("--adj-wake-tol", type=float, default=1e-4,
                     help="adjoint: the same for relative changes (default 1e-4; 0 = exact)")
+    ap.add_argument("--adj-solver", default="sweeps", choices=["sweeps", "causal"],
+                    help="adjoint: reverse sweeps until nothing changes, or one evaluation per "
+                         "cell in reverse causal order")
     ap.add_argument("--fwd-order-filter", type=int, default=1,
                     help="1 (library default): FP32 forward sweeps each brick only in the "
                          "orderings that follow its learned upwind directions; 0: all")

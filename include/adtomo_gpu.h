@@ -164,6 +164,9 @@ int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double
  * --------------------------------------------------------------------- */
 #define ADT_F32 0
 #define ADT_F64 1
+/* adjoint solvers of the batched plan (adt_batch_opts.adj_solver) */
+#define ADT_ADJ_SWEEPS 0 /* reverse sweeps until nothing changes (brick skipping, filters) */
+#define ADT_ADJ_CAUSAL 1 /* one evaluation per cell in reverse causal order */
 /* Receivers per field.  Up to 1024 the seed merge runs in shared memory;
  * above, in device scratch of about 128 bytes per receiver per resident solve. */
 #define ADT_BATCH_MAX_RECEIVERS 65536
@@ -204,6 +207,15 @@ typedef struct adt_batch_opts {
                            chunk at a time.  Not with ref_compat. */
   int32_t adj_warps;    /* adjoint kernel's warps per solve: 0 = as `warps` */
   int32_t adj_groups;   /* adjoint kernel's solves per CTA: 0 = as `groups` */
+  int32_t adj_solver;   /* ADT_ADJ_SWEEPS (default) or ADT_ADJ_CAUSAL: the adjoint
+                           system of a solve is triangular in travel-time order
+                           (a cell's row reads only its users, whose travel times
+                           are larger), so it is solved by evaluating every cell
+                           once, after its users, in rounds of cells whose users
+                           are done (one solve per CTA; adj_warps = warps per CTA,
+                           adj_groups and the adjoint wake tolerance and filter
+                           ignored).  Same formula per cell: the exact sweeps'
+                           fixed point.  Needs fewer than 2^31 cells per field. */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;

@@ -284,7 +284,84 @@ def test_batch_fp32_accuracy_against_fp64():
     B.close()
 
 
-def _fp32_vs_fp64_full_grid(fields, stations, slow, slow_obs, sf, src):
+def test_batch_causal_adjoint_fp64_bit_exact():
+    """The causal-order adjoint (adj_solver "causal") in FP64 with the
+    reference stopping rule: misfit, predicted times and gradient
+    bit-identical to the oracle (whose adjoint is the same substitution in
+    travel-time order), on two fields whose depths are not multiples of 4
+    (the per-cell code passes), a corner source and missing picks."""
+    rng = np.random.default_rng(7)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(20, 17, 13, 0.5), (12, 26, 41, 0.25)], 6, 9)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True,
+                  adj_solver="causal")
+    mis, tp, grads, st = B.run(slow, t_obs, w)
+    mo, tpo, go, ito = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-6, 20)
+    assert np.array_equal(tp, tpo)
+    assert mis == mo
+    for g, r in zip(grads, go):
+        assert np.array_equal(g, r)
+    assert all(s.adj_converged == 1 and s.adj_iters == 1 for s in st)
+    stats = B.stats()
+    assert stats.adj_groups == 1 and stats.adj_bricks == 0
+    assert stats.adj_cell_updates > 0
+    B.close()
+
+
+@pytest.mark.parametrize("dims", [[(40, 36, 24, 0.5), (24, 24, 48, 0.5)],
+                                  [(33, 29, 21, 0.5), (18, 22, 30, 0.4)]],
+                         ids=["l8", "ragged"])
+def test_batch_causal_adjoint_fp32_equals_exact_sweeps(dims):
+    """FP32: the causal-order adjoint evaluates every cell once with the
+    sweeping adjoint's formula, so its gradient equals the exact sweeps'
+    fixed point (adj_wake_tol 0).  Bit for bit where both use the vector
+    code passes and tiles (depths multiple of 8); on ragged depths the sweeps'
+    per-cell tile path sums in another order, so there to 1e-5 relative.
+    Both against the FP64 oracle as well."""
+    rng = np.random.default_rng(11)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(rng, dims, 8, 12)
+    out = {}
+    for solver in ("sweeps", "causal"):
+        B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7,
+                      adj_solver=solver)
+        out[solver] = B.run(slow, t_obs, w)
+        assert all(s.converged and s.adj_converged for s in out[solver][3])
+        B.close()
+    (ms, tps, gs, _), (mc, tpc, gc, stc) = out["sweeps"], out["causal"]
+    assert np.array_equal(tps, tpc) and ms == mc  # same forward
+    assert all(s.adj_iters == 1 for s in stc)
+    exact = all(f[2] % 8 == 0 for f in dims)
+    for a, b in zip(gs, gc):
+        if exact:
+            assert np.array_equal(a, b)
+        else:
+            assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(a)
+    mo, tpo, go, _ = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-12, 100)
+    for g, r in zip(gc, go):
+        assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r)
+
+
+def test_batch_causal_adjoint_chunking_and_overlap():
+    """Chunks of 3 solves, one or two resident: the gradient (FP64 sum in
+    solve order) is the same bits as all solves at once."""
+    rng = np.random.default_rng(12)
+    fields, stations, slow, sf, src, t_obs, w = make_batch(
+        rng, [(32, 28, 24, 0.5), (20, 24, 16, 0.5)], 8, 10)
+    ref = None
+    for kw in ({}, {"chunk": 3}, {"chunk": 3, "overlap_chunks": True}):
+        B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-7,
+                      adj_solver="causal", **kw)
+        mis, tp, grads, st = B.run(slow, t_obs, w)
+        B.close()
+        if ref is None:
+            ref = (mis, tp, grads)
+            continue
+        assert mis == ref[0] and np.array_equal(tp, ref[1]), kw
+        for g, r in zip(grads, ref[2]):
+            assert np.array_equal(g, r), kw
+
+
+def _fp32_vs_fp64_full_grid(fields, stations, slow, slow_obs, sf, src, **kw):
     """FP32 plan with the bench's wake tolerances against the reference's FP64
     op (the oracle: tol 1e-6, 20 iterations, exact causal adjoint) on the same
     picks: FP64 travel times on the perturbed model (the library's FP64 plan
@@ -295,7 +372,7 @@ def _fp32_vs_fp64_full_grid(fields, stations, slow, slow_obs, sf, src):
     _, t_obs, _, _ = P.run(slow_obs, np.full(n_obs, 1.0), w)
     P.close()
     B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, wake_tol=1e-6,
-                  adj_wake_tol=1e-5)
+                  **({"adj_wake_tol": 1e-5} | kw))
     mis, tp, grads, st = B.run(slow, t_obs, w)
     B.close()
     assert all(s.converged and s.adj_converged for s in st)
@@ -321,6 +398,18 @@ def test_batch_fp32_c3_full_grid_against_fp64():
     src = synth.volume_sources(m, n, l, 8, rng)
     f_obs = f / (1.0 + 0.02 * rng.standard_normal(f.shape))
     _fp32_vs_fp64_full_grid([(m, n, l, h)], [sta], [f], [f_obs], np.zeros(8, np.int32), src)
+
+
+def test_batch_fp32_c3_full_grid_causal_adjoint_against_fp64():
+    """As above with the causal-order adjoint (no adjoint wake tolerance)."""
+    rng = np.random.default_rng(0)
+    m, n, l, h = 128, 128, 64, 0.5
+    f = synth.layered_checkerboard(m, n, l, block=8)
+    sta = synth.surface_stations(m, n, 100, rng)
+    src = synth.volume_sources(m, n, l, 8, rng)
+    f_obs = f / (1.0 + 0.02 * rng.standard_normal(f.shape))
+    _fp32_vs_fp64_full_grid([(m, n, l, h)], [sta], [f], [f_obs], np.zeros(8, np.int32), src,
+                            adj_solver="causal")
 
 
 def test_batch_fp32_c4_largest_grid_p_and_s_against_fp64():
