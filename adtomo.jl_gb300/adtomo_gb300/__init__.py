@@ -5,7 +5,7 @@ include/adtomo_gpu.h); this package binds it with ctypes and mirrors the
 reference's Julia API (src/eikonal_op.jl).  There is no CPU fallback: if the
 library cannot be loaded, or no GPU is present, calls raise AdtError.
 """
-from ._lib import ADT_ADJ_CAUSAL, ADT_ADJ_SWEEPS, ADT_F32, ADT_F64, AdtError, lib  # noqa: F401
+from ._lib import ADT_ADJ_AUTO, ADT_ADJ_CAUSAL, ADT_ADJ_SWEEPS, ADT_F32, ADT_F64, AdtError, lib  # noqa: F401
 from .ops import (Batch3D, eikonal, eikonal3d, eikonal3d_grad, eikonal_batch,  # noqa: F401
                   eikonal_grad)
 

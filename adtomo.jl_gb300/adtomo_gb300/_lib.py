@@ -21,7 +21,7 @@ ERRORS = {
     -7: "ADT_ENODEV",
 }
 ADT_F32, ADT_F64 = 0, 1
-ADT_ADJ_SWEEPS, ADT_ADJ_CAUSAL = 0, 1
+ADT_ADJ_SWEEPS, ADT_ADJ_CAUSAL, ADT_ADJ_AUTO = 0, 1, 2
 
 
 class AdtError(RuntimeError):

@@ -14,7 +14,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (ADT_ADJ_CAUSAL, ADT_ADJ_SWEEPS, ADT_F32, ADT_F64, AdtError, BatchOpts,
+from ._lib import (ADT_ADJ_AUTO, ADT_ADJ_CAUSAL, ADT_ADJ_SWEEPS, ADT_F32, ADT_F64, AdtError, BatchOpts,
                    BatchStats, SolveStatus, check, lib)
 
 __all__ = ["eikonal", "eikonal_grad", "eikonal_batch", "eikonal3d", "eikonal3d_grad", "Batch3D",
@@ -127,14 +127,15 @@ class Batch3D:
     skipping) let bricks that moved by at most that much (seconds; relative
     for the adjoint) leave their neighbours asleep.  adj_solver "causal"
     (ADT_ADJ_CAUSAL) solves each adjoint system once in reverse causal order
-    instead of by sweeps ("sweeps", ADT_ADJ_SWEEPS).
+    instead of by sweeps ("sweeps", ADT_ADJ_SWEEPS); "auto" (the default)
+    takes the causal solve in FP64 and the sweeps in FP32.
     """
 
     def __init__(self, fields, stations, solve_field, src_xyz, precision=ADT_F32, tol=1e-6,
                  max_iter=200, adj_max_iter=200, ref_compat=False, near_src_f64=2, chunk=0,
                  bk=0, warps=0, groups=0, use_graph=True, wake_tol=0.0, adj_wake_tol=0.0,
                  adj_order_filter=True, fwd_order_filter=True, overlap_chunks=False,
-                 adj_warps=0, adj_groups=0, adj_solver="sweeps"):
+                 adj_warps=0, adj_groups=0, adj_solver="auto"):
         L = lib()
         self._L = L
         self.fields = [tuple(x) for x in fields]
@@ -158,7 +159,7 @@ class Batch3D:
         o.fwd_order_filter = int(bool(fwd_order_filter))
         o.overlap_chunks = int(bool(overlap_chunks))
         o.adj_warps, o.adj_groups = adj_warps, adj_groups
-        solvers = {"sweeps": ADT_ADJ_SWEEPS, "causal": ADT_ADJ_CAUSAL}
+        solvers = {"sweeps": ADT_ADJ_SWEEPS, "causal": ADT_ADJ_CAUSAL, "auto": ADT_ADJ_AUTO}
         o.adj_solver = solvers[adj_solver] if isinstance(adj_solver, str) else int(adj_solver)
         self._keep = (dims, hs, sta, src)
         h = C.c_void_p()

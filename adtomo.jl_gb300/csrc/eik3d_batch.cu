@@ -224,7 +224,7 @@ void batch_opts_default(adt_batch_opts* o) {
   o->overlap_chunks = 0;
   o->adj_warps = 0;
   o->adj_groups = 0;
-  o->adj_solver = ADT_ADJ_SWEEPS;
+  o->adj_solver = ADT_ADJ_AUTO;
 }
 
 static int enqueue(BatchPlan& P, bool capturing);
@@ -320,8 +320,10 @@ int batch_check_args(int32_t n_fields, const int32_t* dims, const double* hh, co
     return set_error(ADT_EINVAL, "batch: wake_tol and adj_wake_tol must be finite and >= 0");
   if (o.bk != 0 && o.bk != 16 && o.bk != 32 && o.bk != 64)
     return set_error(ADT_EINVAL, "batch: bk must be 0, 16, 32 or 64");
-  if (o.adj_solver != ADT_ADJ_SWEEPS && o.adj_solver != ADT_ADJ_CAUSAL)
-    return set_error(ADT_EINVAL, "batch: adj_solver must be ADT_ADJ_SWEEPS or ADT_ADJ_CAUSAL");
+  if (o.adj_solver != ADT_ADJ_SWEEPS && o.adj_solver != ADT_ADJ_CAUSAL &&
+      o.adj_solver != ADT_ADJ_AUTO)
+    return set_error(ADT_EINVAL, "batch: adj_solver must be ADT_ADJ_AUTO, ADT_ADJ_SWEEPS or "
+                     "ADT_ADJ_CAUSAL");
   return ADT_OK;
 }
 
@@ -354,7 +356,8 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   (void)minl;
   P->bk = o.bk ? o.bk : 32;
   P->nf = n_fields;
-  P->causal = o.adj_solver == ADT_ADJ_CAUSAL;
+  P->causal = o.adj_solver == ADT_ADJ_CAUSAL ||
+              (o.adj_solver == ADT_ADJ_AUTO && o.precision == ADT_F64);
   if (P->causal)
     for (int f = 0; f < n_fields; ++f)
       if ((int64_t)dims[3 * f] * dims[3 * f + 1] * dims[3 * f + 2] >= ((int64_t)1 << 31))

@@ -215,7 +215,7 @@ def gpu_picks(A):
     return tp
 
 
-def fp64_batched_events_per_s(A, t_obs, steps=1, adj_solver="sweeps"):
+def fp64_batched_events_per_s(A, t_obs, steps=1, adj_solver="auto"):
     """The same batched plan in FP64 (exact brick skipping, tol 1e-6, the same
     adjoint solver): the yardstick the FP32 path is measured against.  CUDA
     events around `steps` evaluations after one warm-up."""
@@ -407,8 +407,10 @@ def run_ours(args, rank, world):
                 "fwd_ms": st64.fwd_ms, "adj_ms": st64.adj_ms,
                 "cell_updates": int(st64.fwd_cell_updates + st64.adj_cell_updates),
                 "fp32_over_fp64": value / world / v64,
-                "what": "the same batched plan in FP64 (exact brick skipping, tol 1e-6), "
-                        "256 events, one evaluation after a warm-up, CUDA events"}
+                "what": "the same batched plan in FP64 (tol 1e-6, exact brick skipping in "
+                        f"the forward, adjoint solver '{args.adj_solver}': causal order in FP64 "
+                        "unless 'sweeps'), 256 events, one evaluation after a warm-up, "
+                        "CUDA events"}
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -788,9 +790,10 @@ def main():
                          "(default 1e-6, the stopping tolerance; 0 = exact skipping)")
     ap.add_argument("--adj-wake-tol", type=float, default=1e-4,
                     help="adjoint: the same for relative changes (default 1e-4; 0 = exact)")
-    ap.add_argument("--adj-solver", default="sweeps", choices=["sweeps", "causal"],
-                    help="adjoint: reverse sweeps until nothing changes, or one evaluation per "
-                         "cell in reverse causal order")
+    ap.add_argument("--adj-solver", default="auto", choices=["auto", "sweeps", "causal"],
+                    help="adjoint: reverse sweeps until nothing changes, one evaluation per "
+                         "cell in reverse causal order, or auto (the library default: causal "
+                         "in FP64, sweeps in FP32)")
     ap.add_argument("--fwd-order-filter", type=int, default=1,
                     help="1 (library default): FP32 forward sweeps each brick only in the "
                          "orderings that follow its learned upwind directions; 0: all")

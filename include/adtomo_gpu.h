@@ -167,6 +167,7 @@ int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double
 /* adjoint solvers of the batched plan (adt_batch_opts.adj_solver) */
 #define ADT_ADJ_SWEEPS 0 /* reverse sweeps until nothing changes (brick skipping, filters) */
 #define ADT_ADJ_CAUSAL 1 /* one evaluation per cell in reverse causal order */
+#define ADT_ADJ_AUTO 2   /* causal in FP64, sweeps in FP32 (each the faster there) */
 /* Receivers per field.  Up to 1024 the seed merge runs in shared memory;
  * above, in device scratch of about 128 bytes per receiver per resident solve. */
 #define ADT_BATCH_MAX_RECEIVERS 65536
@@ -207,15 +208,20 @@ typedef struct adt_batch_opts {
                            chunk at a time.  Not with ref_compat. */
   int32_t adj_warps;    /* adjoint kernel's warps per solve: 0 = as `warps` */
   int32_t adj_groups;   /* adjoint kernel's solves per CTA: 0 = as `groups` */
-  int32_t adj_solver;   /* ADT_ADJ_SWEEPS (default) or ADT_ADJ_CAUSAL: the adjoint
-                           system of a solve is triangular in travel-time order
+  int32_t adj_solver;   /* ADT_ADJ_AUTO (default), ADT_ADJ_SWEEPS or ADT_ADJ_CAUSAL:
+                           the adjoint system of a solve is triangular in travel-time order
                            (a cell's row reads only its users, whose travel times
                            are larger), so it is solved by evaluating every cell
                            once, after its users, in rounds of cells whose users
                            are done (one solve per CTA; adj_warps = warps per CTA,
                            adj_groups and the adjoint wake tolerance and filter
                            ignored).  Same formula per cell: the exact sweeps'
-                           fixed point.  Needs fewer than 2^31 cells per field. */
+                           fixed point.  Needs fewer than 2^31 cells per field.
+                           The causal solve gathers each cell's neighbours from
+                           memory, so it is bound by scattered accesses; it wins
+                           where a sweep update is expensive (FP64: 14x on
+                           128x128x64) and loses in FP32, where the sweeps run
+                           from shared-memory tiles. */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;

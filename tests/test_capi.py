@@ -82,7 +82,7 @@ def test_size_mismatch_is_rejected_host_side():
 @pytest.mark.parametrize("kw", [{"wake_tol": -1.0}, {"adj_wake_tol": float("nan")}, {"bk": 8},
                                 {"precision": 7}, {"max_iter": 0}, {"tol": -1.0},
                                 {"ref_compat": True}, {"max_iter": 100001},
-                                {"adj_max_iter": 100001}, {"adj_solver": 2}])
+                                {"adj_max_iter": 100001}, {"adj_solver": 3}])
 def test_batch_options_rejected_host_side(kw):
     with pytest.raises(A.AdtError) as e:
         A.Batch3D([(8, 8, 8, 1.0)], [np.zeros((1, 3))], [0], [[1.0, 1.0, 1.0]], **kw)

@@ -215,7 +215,8 @@ def test_batch_fp64_ref_compat_bit_exact():
     rng = np.random.default_rng(7)
     fields, stations, slow, sf, src, t_obs, w = make_batch(
         rng, [(20, 17, 13, 0.5), (12, 26, 40, 0.25)], 6, 9)
-    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True)
+    B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F64, tol=1e-6, ref_compat=True,
+                  adj_solver="sweeps")
     mis, tp, grads, st = B.run(slow, t_obs, w)
     mo, tpo, go, ito = oracle_batch(fields, stations, slow, sf, src, t_obs, w, 1e-6, 20)
     assert np.array_equal(tp, tpo)
@@ -475,7 +476,7 @@ def test_batch_adjoint_order_filter_is_exact():
         out = []
         for filt in (True, False):
             B = A.Batch3D(fields, stations, sf, src, precision=prec, tol=1e-7,
-                          adj_order_filter=filt)
+                          adj_order_filter=filt, adj_solver="sweeps")
             mis, tp, grads, st = B.run(slow, t_obs, w)
             out.append((mis, tp, grads, B.stats().adj_bricks, st))
             B.close()
