@@ -10,35 +10,44 @@
 // exactly: every cell is evaluated once, after all its users (Kahn's
 // algorithm on that graph).
 //
-// One CTA runs one solve at a time (solves from the chunk's work counter):
-//  - pass 1 forms the side codes and fixed cells, pass 2 the user bits (the
-//    same code passes as the sweeping adjoint) and, per cell, a byte of the
-//    user bits still outstanding (REM_FIXED for a fixed cell, never released);
+// One CTA runs one solve at a time (solves from the chunk's work counter).
+// Per cell the kernel keeps a 32-bit meta word (upwind sides, fixed, seed,
+// user bits, and the user bits still outstanding in bits 16-21) and a record
+// {lambda, upwind difference per axis} (CausalRec):
+//  - pass 1 reads the travel times once (coalesced) and writes the sides,
+//    the fixed flag and the differences; pass 2 the user bits, from the
+//    neighbours' meta words;
 //  - the cells without users are frontier 0 in the solve's queue;
-//  - round r evaluates frontier r.  Each evaluated cell clears its bit in the
-//    byte of each upwind neighbour (atomicAnd on the word of four bytes), and
-//    the thread whose clear empties a byte appends that cell to frontier
-//    r + 1; a CTA barrier ends the round, which publishes the round's adjoint
-//    values and queue entries to the next.
+//  - round r evaluates frontier r from the cell's own record and its users'
+//    records (a user's difference along the axis is its weight u_r - u_c),
+//    and clears its bit in each upwind neighbour's outstanding bits
+//    (atomicAnd on the meta word); the thread whose clear empties them
+//    appends that cell to frontier r + 1.  A CTA barrier ends the round,
+//    which publishes the round's adjoint values and queue entries.
 // On the 128x128x64 layered + checkerboard workload a solve takes about 350
 // rounds of about 3000 cells (2.9 users per cell).
 //
 // A cell is evaluated with the sweeping adjoint's formula, the same
-// operations in the same order (FP32: adj_cell_f32 and the sweep step; FP64:
-// sweep_brick_adj's exact form, which the oracle follows), so the result is
-// the sweeps' exact fixed point, bit for bit (up to the sign of a zero), with
-// one evaluation per cell instead of one per sweep that reaches it.
+// operations in the same order on the same operands (FP32: adj_cell_f32 and
+// the sweep step; FP64: sweep_brick_adj's exact form, which the oracle
+// follows), so the result is the sweeps' exact fixed point, bit for bit (up
+// to the sign of a zero), with one evaluation per cell instead of one per
+// sweep that reaches it.
 #pragma once
 #include "eik3d_batch_kernels.cuh"
 
-// Threads per CTA the kernel is compiled for: FP32 1024 (64 registers, two
-// 512-thread solves per SM), FP64 512 (its doubles need more registers).
+// Threads per CTA the kernel is compiled for: FP32 1024 (64 registers), FP64
+// 512 (its doubles need more registers).
 #ifndef ADT_CAUSAL_MAXT
 #define ADT_CAUSAL_MAXT 1024
 #endif
 #define ADT_CAUSAL_BOUNDS(T) __launch_bounds__(sizeof(T) == 8 ? ADT_CAUSAL_MAXT / 2 : ADT_CAUSAL_MAXT)
 
 namespace adt {
+
+// Meta word: bits 0-15 the adjoint code (adt_common.cuh), bits 16-21 the
+// user bits whose users are not evaluated yet.
+constexpr int META_OUT = 16;
 
 struct CausalShared {
   int q;
@@ -94,28 +103,113 @@ __device__ __forceinline__ T seed_lookup(const int64_t* idx, const T* val, int n
   return val[lo];
 }
 
-// The adjoint value of one non-fixed cell from its neighbours (un: x-, x+,
-// y-, y+, z-, z+; +inf off the grid) and its users' adjoint values (ln, 0
-// for a neighbour that is not a user); gs: the seed value (0 without one).
+// Side code and upwind difference of one axis from the two neighbours (+inf
+// off the grid): the side is the smaller neighbour (ties to +1) when u_c
+// exceeds it (upwind_side_t's rule); the difference u_c - min is formed as
+// the FP32 sweep forms it (fmaxf(u_c - fminf(.), 0)) and, in FP64, as the
+// oracle's diagonal does (u_c - a when active, else 0).
+template <class T>
+__device__ __forceinline__ void axis_side(T uc, T um, T up, uint32_t& side, T& d) {
+  const bool minus = up > um;
+  const T a = minus ? um : up;
+  side = uc > a ? (minus ? 1u : 2u) : 0u;
+  if constexpr (sizeof(T) == 4)
+    d = fmaxf(uc - fminf(um, up), 0.0f);
+  else
+    d = uc > a ? __dsub_rn(uc, a) : 0.0;
+}
+
+// Pass 1 for four consecutive cells (FP32, l % 4 == 0) from p1_load's loads.
+__device__ __forceinline__ void p1_store_causal(const P1Loads& r, uint32_t* meta,
+                                                CausalRec<float>* rec, const SolveDev& sd,
+                                                int64_t x, int i, int j, int k) {
+  const float uc[4] = {r.c4.x, r.c4.y, r.c4.z, r.c4.w};
+  const float vxm[4] = {r.xm.x, r.xm.y, r.xm.z, r.xm.w}, vxp[4] = {r.xp.x, r.xp.y, r.xp.z, r.xp.w};
+  const float vym[4] = {r.ym.x, r.ym.y, r.ym.z, r.ym.w}, vyp[4] = {r.yp.x, r.yp.y, r.yp.z, r.yp.w};
+  uint32_t m[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float um[3] = {vxm[q], vym[q], q == 0 ? r.zm : uc[q - 1]};
+    const float up[3] = {vxp[q], vyp[q], q == 3 ? r.zp : uc[q + 1]};
+    uint32_t cd = 0;
+    CausalRec<float> rc;
+    rc.lam = 0.0f;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      uint32_t side;
+      axis_side(uc[q], um[ax], up[ax], side, rc.d[ax]);
+      cd |= side << (2 * ax);
+    }
+    if (uc[q] == (float)u0_at(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
+    m[q] = cd;
+    rec[x + q] = rc;
+  }
+  *reinterpret_cast<uint4*>(meta + x) = make_uint4(m[0], m[1], m[2], m[3]);
+}
+
+// Pass 2 for four consecutive cells from 16-byte loads of the meta words:
+// user bits (neighbour r uses c when r is not fixed and its side along the
+// axis points at c), written to bits 8-13 and, as outstanding, 16-21.
+// Returns one byte per cell: its user bits, or REM_FIXED for a fixed cell.
+__device__ __forceinline__ uint32_t p2_causal(uint32_t* meta, const Geom& g, int64_t x, int i, int j,
+                                              int k) {
+  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+  auto ld4 = [&](int64_t y) -> uint4 { return *reinterpret_cast<const uint4*>(meta + y); };
+  const uint4 fixed4 = make_uint4(CODE_FIXED, CODE_FIXED, CODE_FIXED, CODE_FIXED);
+  const uint4 c4 = ld4(x);
+  const uint4 xm = i > 0 ? ld4(x - sI) : fixed4, xp = i < g.m - 1 ? ld4(x + sI) : fixed4;
+  const uint4 ym = j > 0 ? ld4(x - sJ) : fixed4, yp = j < g.n - 1 ? ld4(x + sJ) : fixed4;
+  const uint32_t zm = k > 0 ? meta[x - 1] : CODE_FIXED, zp = k + 4 < g.l ? meta[x + 4] : CODE_FIXED;
+  const uint32_t cc[4] = {c4.x, c4.y, c4.z, c4.w};
+  const uint32_t vxm[4] = {xm.x, xm.y, xm.z, xm.w}, vxp[4] = {xp.x, xp.y, xp.z, xp.w};
+  const uint32_t vym[4] = {ym.x, ym.y, ym.z, ym.w}, vyp[4] = {yp.x, yp.y, yp.z, yp.w};
+  auto uses = [](uint32_t cr, int ax, uint32_t want) -> bool {
+    return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
+  };
+  uint32_t out[4], bytes = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t cd = cc[q];
+    if (cd & CODE_FIXED) {
+      bytes |= REM_FIXED << (8 * q);
+    } else {
+      uint32_t us = 0;
+      if (uses(vxm[q], 0, 2u)) us |= 1u;
+      if (uses(vxp[q], 0, 1u)) us |= 2u;
+      if (uses(vym[q], 1, 2u)) us |= 4u;
+      if (uses(vyp[q], 1, 1u)) us |= 8u;
+      if (uses(q == 0 ? zm : cc[q - 1], 2, 2u)) us |= 16u;
+      if (uses(q == 3 ? zp : cc[q + 1], 2, 1u)) us |= 32u;
+      cd |= (us << CODE_USERS) | (us << META_OUT);
+      bytes |= us << (8 * q);
+    }
+    out[q] = cd;
+  }
+  // only bits above the sides and the fixed flag change: a neighbour reading
+  // these words concurrently sees the same low bits either way
+  *reinterpret_cast<uint4*>(meta + x) = make_uint4(out[0], out[1], out[2], out[3]);
+  return bytes;
+}
+
+// The adjoint value of one non-fixed cell: meta word mt, its own upwind
+// differences dc, its users' upwind differences towards it (w, 0 for a
+// neighbour that is not a user) and adjoint values (ln, 0 likewise), in the
+// order x-, x+, y-, y+, z-, z+; gs: the seed value (0 without one).
 // FP32: lambda = fma(P_x + P_y, c2, fma(P_z, c2, c0)), P_a = fma(w_{a+},
 // lambda_{a+}, w_{a-} lambda_{a-}), c2 = rcp(d), c0 = 0.5 g c2 -- the
 // sweeping adjoint's order for every sweep direction (adj_cell_f32).
 // FP64: (g + sum_users 2 (u_r - u_c) lambda_r) / sum_sides 2 (u_c - u_side)
 // in the oracle's order (sweep_brick_adj with EXACT).
 template <class T>
-__device__ __forceinline__ T causal_lambda(uint32_t cd, T uc, const T (&un)[6], const T (&ln)[6],
-                                           T gs) {
+__device__ __forceinline__ T causal_lambda(uint32_t mt, const T (&dc)[3], const T (&w)[6],
+                                           const T (&ln)[6], T gs) {
   if constexpr (sizeof(T) == 4) {
-    const uint32_t us = cd >> CODE_USERS;
-    float w[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) w[q] = ((us >> q) & 1u) ? un[q] - uc : 0.0f;
     const float px = fmaf(w[1], ln[1], w[0] * ln[0]);
     const float py = fmaf(w[3], ln[3], w[2] * ln[2]);
     const float pz = fmaf(w[5], ln[5], w[4] * ln[4]);
-    float d = fmaxf(uc - fminf(un[0], un[1]), 0.0f);
-    d += fmaxf(uc - fminf(un[2], un[3]), 0.0f);
-    d += fmaxf(uc - fminf(un[4], un[5]), 0.0f);
+    float d = dc[0];
+    d += dc[1];
+    d += dc[2];
     const float c2 = rcp_approx(d);
     const float c0 = 0.5f * gs * c2;
     return fmaf(px + py, c2, fmaf(pz, c2, c0));
@@ -123,14 +217,11 @@ __device__ __forceinline__ T causal_lambda(uint32_t cd, T uc, const T (&un)[6], 
     double acc = gs;
 #pragma unroll
     for (int q = 0; q < 6; ++q)
-      if (cd & (1u << (CODE_USERS + q)))
-        acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(2.0, __dsub_rn(un[q], uc)), ln[q]));
+      if (mt & (1u << (CODE_USERS + q))) acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(2.0, w[q]), ln[q]));
     double d = 0.0;
 #pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const uint32_t side = (cd >> (2 * ax)) & 3u;
-      if (side) d = __dadd_rn(d, __dmul_rn(2.0, __dsub_rn(uc, side == 1 ? un[2 * ax] : un[2 * ax + 1])));
-    }
+    for (int ax = 0; ax < 3; ++ax)
+      if ((mt >> (2 * ax)) & 3u) d = __dadd_rn(d, __dmul_rn(2.0, dc[ax]));
     return __ddiv_rn(acc, d);
   }
 }
@@ -141,7 +232,6 @@ template <class T, int NB>
 __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
   __shared__ CausalShared S;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = nth >> 5;
   unsigned long long upd = 0;
   int q = blockIdx.x;
   while (q < A.n_solves) {
@@ -150,55 +240,60 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     const FieldDev<T> fd = A.fields[sd.field];
     const Geom g = fd.g;
     const T* __restrict__ u = A.u + sd.u_off;
-    T* lam = A.lam + sd.u_off;
-    uint16_t* code = A.code + sd.u_off;
-    uint32_t* rem = A.rem + (sd.u_off >> 2);  // u_off is a multiple of 16
-    uint8_t* rem8 = reinterpret_cast<uint8_t*>(rem);
+    uint32_t* meta = A.meta32 + sd.u_off;
+    CausalRec<T>* rec = A.rec + sd.u_off;
     int* queue = A.queue + sd.u_off;
     const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
     const int ncell = (int)g.ncell;
     const bool vec4 = sizeof(T) == 4 && (g.l % 4) == 0;
+    const T INF = inf_value<T>();
     if (tid == 0) {
       S.cnt[0] = S.cnt[1] = S.cnt[2] = 0;
       S.nonfixed = 0;
     }
-    // pass 1: upwind sides and fixed cells; lambda = 0
+    // pass 1: sides, fixed cells, upwind differences; lambda = 0
     if constexpr (sizeof(T) == 4) {
       if (vec4)
         for (int e = tid; e < ncell / 4; e += nth) {
-          const int64_t col = e / (g.l / 4);
-          const int i = (int)(col / g.n), j = (int)(col % g.n), k = (int)(4 * (int64_t)e - col * g.l);
-          p1_store(p1_load(u, g, 4 * (int64_t)e, i, j, k), code, lam, sd, 4 * (int64_t)e, i, j, k);
+          int i, j, k;
+          cell_ijk(4u * (uint32_t)e, g, fd.div_nl, fd.div_l, i, j, k);
+          p1_store_causal(p1_load(u, g, 4 * (int64_t)e, i, j, k), meta, rec, sd, 4 * (int64_t)e, i,
+                          j, k);
         }
     }
     if (!vec4)
-      for (int64_t col = warp; col < (int64_t)g.m * g.n; col += nwarps) {
-        const int i = (int)(col / g.n), j = (int)(col % g.n);
-        for (int k = lane; k < g.l; k += 32) {
-          const int64_t x = col * g.l + k;
-          const T uc = u[x];
-          const int sx = upwind_side_t(u, x, i, g.m, sI, uc);
-          const int sy = upwind_side_t(u, x, j, g.n, sJ, uc);
-          const int sz = upwind_side_t(u, x, k, g.l, (int64_t)1, uc);
-          uint16_t cd = (uint16_t)(sx | (sy << 2) | (sz << 4));
-          if (uc == (T)u0_at(sd, i, j, k) || (sx | sy | sz) == 0) cd = CODE_FIXED;
-          code[x] = cd;
-          lam[x] = T(0);
+      for (int x = tid; x < ncell; x += nth) {
+        int i, j, k;
+        cell_ijk((uint32_t)x, g, fd.div_nl, fd.div_l, i, j, k);
+        const T uc = u[x];
+        const T un[6] = {i > 0 ? u[x - sI] : INF, i < g.m - 1 ? u[x + sI] : INF,
+                         j > 0 ? u[x - sJ] : INF, j < g.n - 1 ? u[x + sJ] : INF,
+                         k > 0 ? u[x - 1] : INF, k < g.l - 1 ? u[x + 1] : INF};
+        uint32_t cd = 0;
+        CausalRec<T> rc;
+        rc.lam = T(0);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          uint32_t side;
+          axis_side(uc, un[2 * ax], un[2 * ax + 1], side, rc.d[ax]);
+          cd |= side << (2 * ax);
         }
+        if (uc == (T)u0_at(sd, i, j, k) || cd == 0) cd = CODE_FIXED;
+        meta[x] = cd;
+        rec[x] = rc;
       }
     __syncthreads();
-    // pass 2: user bits, outstanding-user bytes, frontier 0 (the cells nobody
-    // uses).  Warp-uniform loops (warp_append needs all lanes).
+    // pass 2: user bits and frontier 0 (the cells nobody uses).  Warp-uniform
+    // loops (warp_append needs all lanes).
     int nf = 0;
     if (vec4) {
       for (int e0 = warp * 32; e0 < ncell / 4; e0 += nth) {
         const int e = e0 + lane;
         uint32_t bytes = 0x80808080u;
         if (e < ncell / 4) {
-          const int64_t col = e / (g.l / 4);
-          const int i = (int)(col / g.n), j = (int)(col % g.n), k = (int)(4 * (int64_t)e - col * g.l);
-          bytes = p2_store(p2_load(code, g, 4 * (int64_t)e, i, j, k), code, 4 * (int64_t)e);
-          rem[e] = bytes;
+          int i, j, k;
+          cell_ijk(4u * (uint32_t)e, g, fd.div_nl, fd.div_l, i, j, k);
+          bytes = p2_causal(meta, g, 4 * (int64_t)e, i, j, k);
         }
         int np = 0;
 #pragma unroll
@@ -219,25 +314,23 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
         if (x < ncell) {
           int i, j, k;
           cell_ijk((uint32_t)x, g, fd.div_nl, fd.div_l, i, j, k);
-          const uint16_t cd = code[x];
+          const uint32_t cd = meta[x];
           if (!(cd & CODE_FIXED)) {
-            uint32_t us = 0;
-            auto uses = [&](int64_t r, int ax, int want) -> bool {
-              const uint16_t cr = code[r];
-              return !(cr & CODE_FIXED) && (((cr >> (2 * ax)) & 3) == want);
+            auto uses = [&](int64_t r, int ax, uint32_t want) -> bool {
+              const uint32_t cr = meta[r];
+              return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
             };
-            if (i > 0 && uses(x - sI, 0, 2)) us |= 1;
-            if (i < g.m - 1 && uses(x + sI, 0, 1)) us |= 2;
-            if (j > 0 && uses(x - sJ, 1, 2)) us |= 4;
-            if (j < g.n - 1 && uses(x + sJ, 1, 1)) us |= 8;
-            if (k > 0 && uses(x - 1, 2, 2)) us |= 16;
-            if (k < g.l - 1 && uses(x + 1, 2, 1)) us |= 32;
-            // only the high bits change: a neighbour reading this code
-            // concurrently sees the same side bits either way
-            code[x] = (uint16_t)(cd | (us << CODE_USERS));
+            uint32_t us = 0;
+            if (i > 0 && uses(x - sI, 0, 2u)) us |= 1u;
+            if (i < g.m - 1 && uses(x + sI, 0, 1u)) us |= 2u;
+            if (j > 0 && uses(x - sJ, 1, 2u)) us |= 4u;
+            if (j < g.n - 1 && uses(x + sJ, 1, 1u)) us |= 8u;
+            if (k > 0 && uses(x - 1, 2, 2u)) us |= 16u;
+            if (k < g.l - 1 && uses(x + 1, 2, 1u)) us |= 32u;
+            // only the high bits change (see p2_causal)
+            meta[x] = cd | (us << CODE_USERS) | (us << META_OUT);
             by = us;
           }
-          rem8[x] = (uint8_t)by;
         }
         nf += by != REM_FIXED;
         const int pos = warp_append(by == 0u ? 1 : 0, &S.cnt[0], lane);
@@ -253,15 +346,14 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     const T* sval = A.seed_val + sd.seed_off;
     for (int e = tid; e < ns; e += nth) {
       const int64_t x = sidx[e];
-      const uint16_t cd = code[x];
-      if (!(cd & CODE_FIXED)) code[x] = (uint16_t)(cd | CODE_SEED);
+      const uint32_t cd = meta[x];
+      if (!(cd & CODE_FIXED)) meta[x] = cd | CODE_SEED;
     }
     __syncthreads();
     // rounds
-    const T INF = inf_value<T>();
     const int st3[3] = {(int)sI, (int)sJ, 1};
-    int base = 0;
-    for (int r = 0;; ++r) {
+    int base = 0, r = 0;
+    for (;; ++r) {
       const int size = S.cnt[r % 3];
       if (size == 0) break;
       if (tid == 0) S.cnt[(r + 2) % 3] = 0;  // frontier r - 1's, read by all before the last barrier
@@ -276,26 +368,18 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
           ok[b] = e < size;
           x[b] = ok[b] ? queue[base + e] : 0;
         }
-        uint32_t cd[NB];
-        T uc[NB], un[NB][6];
+        uint32_t mt[NB];
+        T dc[NB][3];
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
-          cd[b] = 0u;
-          uc[b] = T(0);
-#pragma unroll
-          for (int t = 0; t < 6; ++t) un[b][t] = INF;
+          mt[b] = 0u;
+          dc[b][0] = dc[b][1] = dc[b][2] = T(0);
           if (ok[b]) {
-            int i, j, k;
-            cell_ijk((uint32_t)x[b], g, fd.div_nl, fd.div_l, i, j, k);
-            const T* p = u + x[b];
-            cd[b] = code[x[b]];
-            uc[b] = __ldg(p);
-            if (i > 0) un[b][0] = __ldg(p - sI);
-            if (i < g.m - 1) un[b][1] = __ldg(p + sI);
-            if (j > 0) un[b][2] = __ldg(p - sJ);
-            if (j < g.n - 1) un[b][3] = __ldg(p + sJ);
-            if (k > 0) un[b][4] = __ldg(p - 1);
-            if (k < g.l - 1) un[b][5] = __ldg(p + 1);
+            mt[b] = meta[x[b]];
+            const CausalRec<T> rc = rec[x[b]];
+            dc[b][0] = rc.d[0];
+            dc[b][1] = rc.d[1];
+            dc[b][2] = rc.d[2];
           }
         }
         // release the upwind neighbours (their outstanding bit for this cell)
@@ -305,41 +389,49 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
         for (int b = 0; b < NB; ++b)
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const uint32_t side = (cd[b] >> (2 * a)) & 3u;
+            const uint32_t side = (mt[b] >> (2 * a)) & 3u;
             if (side) {
               const int tq = x[b] + (side == 1 ? -st3[a] : st3[a]);
               const uint32_t bit = side == 1 ? (2u << (2 * a)) : (1u << (2 * a));
-              const uint32_t sh = 8u * ((uint32_t)tq & 3u);
-              const uint32_t old = atomicAnd_block(rem + (tq >> 2), ~(bit << sh));
-              const uint32_t ob = (old >> sh) & 0xffu;
+              const uint32_t old = atomicAnd_block(meta + tq, ~(bit << META_OUT));
+              const uint32_t ob = (old >> META_OUT) & 0x3fu;
               if ((ob & bit) && !(ob & ~bit)) {
                 rel |= 1u << (3 * b + a);
                 ++np;
+                // its record is first read in the next round: fetch it into
+                // L2 now, off that round's dependency chain
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(rec + tq));
               }
             }
           }
-        // the users' adjoint values (final: evaluated in earlier rounds)
-        T ln[NB][6];
+        // the users' records: adjoint value (final: evaluated in an earlier
+        // round) and upwind difference towards this cell (its weight)
+        T w[NB][6], ln[NB][6];
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
-          const uint32_t us = cd[b] >> CODE_USERS;
+          const uint32_t us = mt[b] >> CODE_USERS;
 #pragma unroll
           for (int t = 0; t < 6; ++t) {
-            const int off = (t & 1 ? 1 : -1) * st3[t >> 1];
-            ln[b][t] = ((us >> t) & 1u) ? lam[x[b] + off] : T(0);
+            w[b][t] = T(0);
+            ln[b][t] = T(0);
+            if ((us >> t) & 1u) {
+              const CausalRec<T> rr = rec[x[b] + (t & 1 ? 1 : -1) * st3[t >> 1]];
+              w[b][t] = rr.d[t >> 1];
+              ln[b][t] = rr.lam;
+            }
           }
         }
 #pragma unroll
         for (int b = 0; b < NB; ++b)
           if (ok[b]) {
             T gs = T(0);
-            if (cd[b] & CODE_SEED) {
+            if (mt[b] & CODE_SEED) {
               if constexpr (sizeof(T) == 4)
                 gs = A.gdense ? A.gdense[sd.u_off + x[b]] : seed_lookup(sidx, sval, ns, (int64_t)x[b]);
               else
                 gs = seed_lookup(sidx, sval, ns, (int64_t)x[b]);
             }
-            lam[x[b]] = causal_lambda<T>(cd[b], uc[b], un[b], ln[b], gs);
+            rec[x[b]].lam = causal_lambda<T>(mt[b], dc[b], w[b], ln[b], gs);
           }
         int pos = nbase + warp_append(np, len, lane);
 #pragma unroll
@@ -347,7 +439,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
 #pragma unroll
           for (int a = 0; a < 3; ++a)
             if ((rel >> (3 * b + a)) & 1u) {
-              const uint32_t side = (cd[b] >> (2 * a)) & 3u;
+              const uint32_t side = (mt[b] >> (2 * a)) & 3u;
               queue[pos++] = x[b] + (side == 1 ? -st3[a] : st3[a]);
             }
       }
@@ -358,7 +450,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
       for (int e = tid; e < ns; e += nth) A.gdense[sd.u_off + sidx[e]] = T(0);
     if (tid == 0) {
       adt_solve_status& st = A.status[sd.gidx];
-      st.adj_iters = 1;
+      st.adj_iters = r;  // rounds
       st.adj_converged = base == S.nonfixed ? 1 : 0;  // else the users graph had a cycle
       upd += (unsigned long long)base;
       S.q = atomicAdd(A.next, 1) + (int)gridDim.x;

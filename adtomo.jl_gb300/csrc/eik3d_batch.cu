@@ -170,7 +170,7 @@ struct BatchPlan {
     DevBuf u, lam, code, meta, sidx, sval;
     DevBuf gdense;       // FP32 path: seed values as a dense field per chunk solve (zero elsewhere)
     DevBuf mis_scratch;  // seed merge arrays when they exceed shared memory
-    DevBuf rem, queue;   // causal-order adjoint: outstanding-user bytes and frontiers
+    DevBuf meta32, rec, queue;  // causal-order adjoint: meta words, records, frontiers
   };
   ChunkBufs cb[2];
   int nsets = 1;
@@ -484,8 +484,10 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   for (int k = 0; k < P->nsets; ++k) {
     BatchPlan::ChunkBufs& B = P->cb[k];
     R_(B.u, (size_t)max_cells * es);
-    R_(B.lam, (size_t)max_cells * es);
-    R_(B.code, (size_t)max_cells * 2);
+    if (!P->causal) {  // the causal-order adjoint keeps lambda in its records
+      R_(B.lam, (size_t)max_cells * es);
+      R_(B.code, (size_t)max_cells * 2);
+    }
     R_(B.meta, (size_t)max_bricks * 4);
     R_(B.sidx, (size_t)std::max<int64_t>(max_seeds, 1) * 8);
     R_(B.sval, (size_t)std::max<int64_t>(max_seeds, 1) * es);
@@ -494,7 +496,8 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       ADT_CUDA(cudaMemset(B.gdense.p, 0, (size_t)max_cells * es));
     }
     if (P->causal) {
-      R_(B.rem, (size_t)max_cells);
+      R_(B.meta32, (size_t)max_cells * 4);
+      R_(B.rec, (size_t)max_cells * 4 * es);
       R_(B.queue, (size_t)max_cells * 4);
     }
   }
@@ -669,7 +672,8 @@ static BatchArgs<T> make_args(BatchPlan& P, const BatchPlan::Chunk& ch, int whic
   A.max_nb = P.max_nb;
   A.adj_order_filter = P.opts.adj_order_filter ? 1 : 0;
   A.fwd_order_filter = (!P.f64 && P.opts.fwd_order_filter) ? 1 : 0;
-  A.rem = P.causal ? CB.rem.as<uint32_t>() : nullptr;
+  A.meta32 = P.causal ? CB.meta32.as<uint32_t>() : nullptr;
+  A.rec = P.causal ? CB.rec.as<CausalRec<T>>() : nullptr;
   A.queue = P.causal ? CB.queue.as<int>() : nullptr;
   return A;
 }
@@ -734,14 +738,16 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
     for (int f = 0; f < P.nf; ++f) {
       const int cnt = (int)ch.field_uoff[f].size();
       if (!cnt) continue;
-      const T* lam = P.cb[set].lam.as<T>();
+      // lambda: the sweeps' array, or the causal-order adjoint's records
+      const T* lam = P.causal ? P.cb[set].rec.as<T>() : P.cb[set].lam.as<T>();
+      int lam_stride = P.causal ? 4 : 1;
       const int64_t* uo = P.d_uoff.as<int64_t>() + ch.dev_uoff_off[f];
       const double* f64 = P.d_slow64.as<double>() + P.cell_off[f];
       double hh = P.h[f];
       int64_t nc = P.geoms[f].ncell;
       double* gr = P.d_grad.as<double>() + P.cell_off[f];
       int cc = cnt;
-      void* args[] = {&lam, &uo, &cc, &f64, &hh, &nc, &gr};
+      void* args[] = {&lam, &lam_stride, &uo, &cc, &f64, &hh, &nc, &gr};
       ADT_CUDA(cudaLaunchKernel(P.ks.grad, dim3(grid1d(nc)), dim3(256), args, 0, st));
     }
     if (P.nsets == 2) ADT_CUDA(cudaEventRecord(P.ev_sync[c + 1], st));

@@ -57,6 +57,16 @@ struct SolveDev {
   int64_t seed_off;         // seed slot offset (8 per station) in the chunk seed buffer
 };
 
+// Per-cell record of the causal-order adjoint (eik3d_adj_causal.cuh): the
+// adjoint value and the cell's active upwind difference along each axis,
+// u_c - min(neighbours) (0 when the axis is inactive).  A user r of cell c
+// along axis a has c as its smaller neighbour there, so r's difference along
+// a is exactly u_r - u_c: the records hold every weight of the adjoint rows.
+template <class T>
+struct alignas(4 * sizeof(T)) CausalRec {
+  T lam, d[3];
+};
+
 template <class T>
 struct BatchArgs {
   const FieldDev<T>* fields;
@@ -90,7 +100,8 @@ struct BatchArgs {
   int adj_order_filter;     // 1: adjoint sweeps a brick only in the orderings its flow allows
   int fwd_order_filter;     // 1: FP32 forward sweeps a brick only in the orderings its
                             //    learned upwind directions allow
-  uint32_t* rem;            // causal-order adjoint: outstanding-user bytes, one per chunk cell
+  uint32_t* meta32;         // causal-order adjoint: per chunk cell, code bits and outstanding users
+  CausalRec<T>* rec;        // causal-order adjoint: per chunk cell, lambda and upwind differences
   int* queue;               // causal-order adjoint: frontiers, one int per chunk cell
 };
 
@@ -1119,10 +1130,13 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
 //   order, carried across chunks in grad) and k_grad_scale multiplies by
 //   -2 f h h once after the last chunk: half the FP64 operations, no less
 //   accurate, and the same bits however the solves are chunked.
-// Loads are issued eight solves ahead of the adds.
+// Loads are issued eight solves ahead of the adds.  lambda of cell c of the
+// solve at u_off is lam[(u_off + c) * lam_stride]: stride 1 for the sweeps'
+// lambda array, 4 for the causal-order adjoint's records.
 template <class T>
-__global__ void k_batch_grad(const T* __restrict__ lam, const int64_t* __restrict__ u_off,
-                             int n_solves, const double* __restrict__ f64, double h, int64_t ncell,
+__global__ void k_batch_grad(const T* __restrict__ lam, int lam_stride,
+                             const int64_t* __restrict__ u_off, int n_solves,
+                             const double* __restrict__ f64, double h, int64_t ncell,
                              double* __restrict__ grad) {
   constexpr int U = 8;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
@@ -1134,13 +1148,13 @@ __global__ void k_batch_grad(const T* __restrict__ lam, const int64_t* __restric
     for (; s + U <= n_solves; s += U) {
       double l[U];
 #pragma unroll
-      for (int q = 0; q < U; ++q) l[q] = (double)lam[u_off[s + q] + c];
+      for (int q = 0; q < U; ++q) l[q] = (double)lam[(u_off[s + q] + c) * lam_stride];
 #pragma unroll
       for (int q = 0; q < U; ++q)
         G = sizeof(T) == 4 ? __dadd_rn(G, -l[q]) : __dadd_rn(G, __dmul_rn(-l[q], rhs));
     }
     for (; s < n_solves; ++s) {
-      const double l = (double)lam[u_off[s] + c];
+      const double l = (double)lam[(u_off[s] + c) * lam_stride];
       G = sizeof(T) == 4 ? __dadd_rn(G, -l) : __dadd_rn(G, __dmul_rn(-l, rhs));
     }
     grad[c] = G;
