@@ -140,7 +140,7 @@ __device__ __forceinline__ void p1_store_causal(const P1Loads& r, uint32_t* meta
       axis_side(uc[q], um[ax], up[ax], side, rc.d[ax]);
       cd |= side << (2 * ax);
     }
-    if (uc[q] == (float)u0_at(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
+    if (uc[q] == u0_t<float>(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
     m[q] = cd;
     rec[x + q] = rc;
   }
@@ -278,7 +278,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
           axis_side(uc, un[2 * ax], un[2 * ax + 1], side, rc.d[ax]);
           cd |= side << (2 * ax);
         }
-        if (uc == (T)u0_at(sd, i, j, k) || cd == 0) cd = CODE_FIXED;
+        if (uc == u0_t<T>(sd, i, j, k) || cd == 0) cd = CODE_FIXED;
         meta[x] = cd;
         rec[x] = rc;
       }
@@ -398,9 +398,6 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
               if ((ob & bit) && !(ob & ~bit)) {
                 rel |= 1u << (3 * b + a);
                 ++np;
-                // its record is first read in the next round: fetch it into
-                // L2 now, off that round's dependency chain
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(rec + tq));
               }
             }
           }

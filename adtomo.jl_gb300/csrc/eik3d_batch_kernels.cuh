@@ -142,16 +142,20 @@ __host__ __device__ inline size_t group_hdr_bytes(int G, int meta_smem, int max_
   return b;
 }
 
-// Initial value of the implicit u0: 1000, or the FP64 near-source value at
-// the 8 nodes around the source (k_src_init; scripts/gene_obs.jl:42-51,
-// scripts/inversion.jl:52-60).
-__device__ __forceinline__ double u0_at(const SolveDev& s, int i, int j, int k) {
+// Initial value of the implicit u0 in the compute precision: 1000, or the
+// FP64 near-source value at the 8 nodes around the source (k_src_init;
+// scripts/gene_obs.jl:42-51, scripts/inversion.jl:52-60), converted.  Only
+// those eight nodes convert; every other cell takes the constant.
+template <class T>
+__device__ __forceinline__ T u0_t(const SolveDev& s, int i, int j, int k) {
   const bool xi = (i == s.xc) || (i == s.xf);
   const bool yj = (j == s.yc) || (j == s.yf);
   const bool zk = (k == s.zc) || (k == s.zf);
-  if (!(xi && yj && zk)) return 1000.0;
-  const int a = (i == s.xc) ? 0 : 1, b = (j == s.yc) ? 0 : 1, c = (k == s.zc) ? 0 : 1;
-  return s.v0[a * 4 + b * 2 + c];
+  if (__builtin_expect(xi && yj && zk, 0)) {
+    const int a = (i == s.xc) ? 0 : 1, b = (j == s.yc) ? 0 : 1, c = (k == s.zc) ? 0 : 1;
+    return (T)s.v0[a * 4 + b * 2 + c];
+  }
+  return T(1000);
 }
 
 template <class T>
@@ -492,7 +496,7 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
     for (int64_t col = c.gw; col < (int64_t)g.m * g.n; col += c.GW) {
       const int i = (int)(col / g.n), j = (int)(col % g.n);
       T* uc = u + col * g.l;
-      for (int k = lane; k < g.l; k += 32) uc[k] = (T)u0_at(sd, i, j, k);
+      for (int k = lane; k < g.l; k += 32) uc[k] = u0_t<T>(sd, i, j, k);
     }
     // Only the bricks whose cells or halo hold a source node start dirty.
     // Every other cell starts at 1000 with all its neighbours at 1000, and
@@ -829,7 +833,7 @@ __device__ __forceinline__ void p1_store(const P1Loads& r, uint16_t* code, float
       const float a = minus ? um[ax] : up[ax];
       cd |= (uc[q] > a ? (minus ? 1u : 2u) : 0u) << (2 * ax);
     }
-    if (uc[q] == (float)u0_at(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
+    if (uc[q] == u0_t<float>(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
     packed[q >> 1] |= cd << (16 * (q & 1));
   }
   *reinterpret_cast<uint2*>(code + x) = make_uint2(packed[0], packed[1]);
@@ -978,7 +982,7 @@ __global__ void k_batch_adj(BatchArgs<T> A) {
         const int sy = upwind_side_t(u, x, j, g.n, sJ, uc);
         const int sz = upwind_side_t(u, x, k, g.l, (int64_t)1, uc);
         uint16_t cd = (uint16_t)(sx | (sy << 2) | (sz << 4));
-        if (uc == (T)u0_at(sd, i, j, k) || (sx | sy | sz) == 0) cd = CODE_FIXED;
+        if (uc == u0_t<T>(sd, i, j, k) || (sx | sy | sz) == 0) cd = CODE_FIXED;
         code[x] = cd;
         lam[x] = T(0);
       }
