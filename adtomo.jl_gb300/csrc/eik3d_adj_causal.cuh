@@ -17,15 +17,24 @@
 //  - pass 1 reads the travel times once (coalesced) and writes the sides,
 //    the fixed flag and the differences; pass 2 the user bits, from the
 //    neighbours' meta words;
-//  - the cells without users are frontier 0 in the solve's queue;
-//  - round r evaluates frontier r from the cell's own record and its users'
-//    records (a user's difference along the axis is its weight u_r - u_c),
-//    and clears its bit in each upwind neighbour's outstanding bits
-//    (atomicAnd on the meta word); the thread whose clear empties them
-//    appends that cell to frontier r + 1.  A CTA barrier ends the round,
-//    which publishes the round's adjoint values and queue entries.
-// On the 128x128x64 layered + checkerboard workload a solve takes about 350
-// rounds of about 3000 cells (2.9 users per cell).
+//  - the cells without users open the solve's queue (every slot starts at -1);
+//  - every thread then takes the next queue slot, waits until a cell is
+//    written there, evaluates it from its own record and its users' records
+//    (a user's difference along the axis is its weight u_r - u_c) and clears
+//    its bit in each upwind neighbour's outstanding bits (atomicAnd on the
+//    meta word); the thread whose clear empties them appends that cell to the
+//    queue.  No barrier between cells: a cell is evaluated as soon as its last
+//    user is and a thread has taken its slot.
+// Ordering: a cell's adjoint value is stored before its release atomics,
+// which are acq_rel at CTA scope, and the releasing thread writes the queue
+// slot with a release store that the evaluating thread reads with an acquire
+// load, so every user's value is visible when the cell is evaluated.
+// Progress: slots are taken and written in order, and while a taken slot is
+// unwritten some cell is still unevaluated; the unevaluated cell with the
+// largest travel time has all its users evaluated, so it has been queued and
+// its slot's thread can go on.  Every wait is also bounded
+// (CAUSAL_WAIT_CYCLES); one that runs out marks the solve unconverged instead
+// of hanging, and the other waits then stop too.
 //
 // A cell is evaluated with the sweeping adjoint's formula, the same
 // operations in the same order on the same operands (FP32: adj_cell_f32 and
@@ -51,10 +60,48 @@ constexpr int META_OUT = 16;
 
 struct CausalShared {
   int q;
-  int cnt[3];    // frontier sizes: frontier r's in cnt[r % 3]
-  int nonfixed;  // non-fixed cells of the running solve (each is evaluated once)
+  int head;      // next queue slot to take
+  int tail;      // queue slots written so far
+  int nonfixed;  // non-fixed cells of the running solve (each is queued once)
+  int err;       // a wait on a queue slot ran out of its budget
   int pad;
 };
+
+// A wait on one queue slot gives up after this many SM cycles (about two
+// seconds; a slot is written once the cells queued before it are evaluated,
+// which takes microseconds to milliseconds).
+constexpr long long CAUSAL_WAIT_CYCLES = 4000000000LL;
+
+// CTA-scope acquire load / release store / acq_rel atomic AND on global memory.
+__device__ __forceinline__ int ld_acquire_cta(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta(int* p, int v) {
+  asm volatile("st.release.cta.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t atom_and_acq_rel_cta(uint32_t* p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.cta.global.and.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+// The lanes that arrive together take consecutive slots of a shared counter:
+// n (0..3) each; one shared atomic per group of lanes.  Callable from
+// divergent code (the group is __activemask()).
+__device__ __forceinline__ int take_slots(int n, int* counter) {
+  const unsigned mask = __activemask();
+  const int lane = threadIdx.x & 31;
+  const unsigned b0 = __ballot_sync(mask, n & 1), b1 = __ballot_sync(mask, n & 2);
+  const unsigned lower = (1u << lane) - 1u;
+  const int total = __popc(b0) + 2 * __popc(b1);
+  const int leader = __ffs(mask) - 1;
+  int base = 0;
+  if (lane == leader && total) base = atomicAdd(counter, total);
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(b0 & lower) + 2 * __popc(b1 & lower);
+}
 
 // All 32 lanes call with their entry counts; returns this lane's first slot
 // in a list whose length is counted in *len (one shared atomic per warp).
@@ -226,9 +273,7 @@ __device__ __forceinline__ T causal_lambda(uint32_t mt, const T (&dc)[3], const 
   }
 }
 
-// NB: queue entries per thread per pass over a frontier (their loads are
-// issued together).
-template <class T, int NB>
+template <class T>
 __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
   __shared__ CausalShared S;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -248,8 +293,9 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     const bool vec4 = sizeof(T) == 4 && (g.l % 4) == 0;
     const T INF = inf_value<T>();
     if (tid == 0) {
-      S.cnt[0] = S.cnt[1] = S.cnt[2] = 0;
+      S.head = S.tail = 0;
       S.nonfixed = 0;
+      S.err = 0;
     }
     // pass 1: sides, fixed cells, upwind differences; lambda = 0
     if constexpr (sizeof(T) == 4) {
@@ -259,6 +305,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
           cell_ijk(4u * (uint32_t)e, g, fd.div_nl, fd.div_l, i, j, k);
           p1_store_causal(p1_load(u, g, 4 * (int64_t)e, i, j, k), meta, rec, sd, 4 * (int64_t)e, i,
                           j, k);
+          *reinterpret_cast<int4*>(queue + 4 * (int64_t)e) = make_int4(-1, -1, -1, -1);
         }
     }
     if (!vec4)
@@ -281,6 +328,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
         if (uc == u0_t<T>(sd, i, j, k) || cd == 0) cd = CODE_FIXED;
         meta[x] = cd;
         rec[x] = rc;
+        queue[x] = -1;
       }
     __syncthreads();
     // pass 2: user bits and frontier 0 (the cells nobody uses).  Warp-uniform
@@ -302,7 +350,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
           np += by == 0u;
           nf += by != REM_FIXED;
         }
-        int pos = warp_append(np, &S.cnt[0], lane);
+        int pos = warp_append(np, &S.tail, lane);
 #pragma unroll
         for (int b = 0; b < 4; ++b)
           if (((bytes >> (8 * b)) & 0xffu) == 0u) queue[pos++] = 4 * e + b;
@@ -333,7 +381,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
           }
         }
         nf += by != REM_FIXED;
-        const int pos = warp_append(by == 0u ? 1 : 0, &S.cnt[0], lane);
+        const int pos = warp_append(by == 0u ? 1 : 0, &S.tail, lane);
         if (by == 0u) queue[pos] = x;
       }
     }
@@ -350,106 +398,84 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
       if (!(cd & CODE_FIXED)) meta[x] = cd | CODE_SEED;
     }
     __syncthreads();
-    // rounds
+    // evaluation in causal order
     const int st3[3] = {(int)sI, (int)sJ, 1};
-    int base = 0, r = 0;
-    for (;; ++r) {
-      const int size = S.cnt[r % 3];
-      if (size == 0) break;
-      if (tid == 0) S.cnt[(r + 2) % 3] = 0;  // frontier r - 1's, read by all before the last barrier
-      int* len = &S.cnt[(r + 1) % 3];
-      const int nbase = base + size;
-      for (int e0 = 0; e0 < size; e0 += NB * nth) {
-        int x[NB];
-        bool ok[NB];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-          const int e = e0 + b * nth + tid;
-          ok[b] = e < size;
-          x[b] = ok[b] ? queue[base + e] : 0;
+    const int nonfixed = S.nonfixed;
+    for (;;) {
+      const int slot = take_slots(1, &S.head);
+      if (slot >= nonfixed) break;
+      int x = ld_acquire_cta(queue + slot);
+      if (x < 0) {
+        const long long t0 = clock64();
+        do {
+          __nanosleep(64);
+          x = ld_acquire_cta(queue + slot);
+        } while (x < 0 && clock64() - t0 < CAUSAL_WAIT_CYCLES &&
+                 !*reinterpret_cast<volatile int*>(&S.err));
+        if (x < 0) {  // out of budget, or another thread's was
+          atomicOr(&S.err, 1);
+          break;
         }
-        uint32_t mt[NB];
-        T dc[NB][3];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-          mt[b] = 0u;
-          dc[b][0] = dc[b][1] = dc[b][2] = T(0);
-          if (ok[b]) {
-            mt[b] = meta[x[b]];
-            const CausalRec<T> rc = rec[x[b]];
-            dc[b][0] = rc.d[0];
-            dc[b][1] = rc.d[1];
-            dc[b][2] = rc.d[2];
-          }
-        }
-        // release the upwind neighbours (their outstanding bit for this cell)
-        uint32_t rel = 0;
-        int np = 0;
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const uint32_t side = (mt[b] >> (2 * a)) & 3u;
-            if (side) {
-              const int tq = x[b] + (side == 1 ? -st3[a] : st3[a]);
-              const uint32_t bit = side == 1 ? (2u << (2 * a)) : (1u << (2 * a));
-              const uint32_t old = atomicAnd_block(meta + tq, ~(bit << META_OUT));
-              const uint32_t ob = (old >> META_OUT) & 0x3fu;
-              if ((ob & bit) && !(ob & ~bit)) {
-                rel |= 1u << (3 * b + a);
-                ++np;
-              }
-            }
-          }
-        // the users' records: adjoint value (final: evaluated in an earlier
-        // round) and upwind difference towards this cell (its weight)
-        T w[NB][6], ln[NB][6];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-          const uint32_t us = mt[b] >> CODE_USERS;
-#pragma unroll
-          for (int t = 0; t < 6; ++t) {
-            w[b][t] = T(0);
-            ln[b][t] = T(0);
-            if ((us >> t) & 1u) {
-              const CausalRec<T> rr = rec[x[b] + (t & 1 ? 1 : -1) * st3[t >> 1]];
-              w[b][t] = rr.d[t >> 1];
-              ln[b][t] = rr.lam;
-            }
-          }
-        }
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-          if (ok[b]) {
-            T gs = T(0);
-            if (mt[b] & CODE_SEED) {
-              if constexpr (sizeof(T) == 4)
-                gs = A.gdense ? A.gdense[sd.u_off + x[b]] : seed_lookup(sidx, sval, ns, (int64_t)x[b]);
-              else
-                gs = seed_lookup(sidx, sval, ns, (int64_t)x[b]);
-            }
-            rec[x[b]].lam = causal_lambda<T>(mt[b], dc[b], w[b], ln[b], gs);
-          }
-        int pos = nbase + warp_append(np, len, lane);
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-            if ((rel >> (3 * b + a)) & 1u) {
-              const uint32_t side = (mt[b] >> (2 * a)) & 3u;
-              queue[pos++] = x[b] + (side == 1 ? -st3[a] : st3[a]);
-            }
       }
-      __syncthreads();
-      base = nbase;
+      const uint32_t mt = meta[x];
+      const CausalRec<T> rc = rec[x];
+      const T dc[3] = {rc.d[0], rc.d[1], rc.d[2]};
+      // the users' records: adjoint value (final) and upwind difference
+      // towards this cell (its weight)
+      T w[6], ln[6];
+      const uint32_t us = mt >> CODE_USERS;
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        w[t] = T(0);
+        ln[t] = T(0);
+        if ((us >> t) & 1u) {
+          const CausalRec<T> rr = rec[x + (t & 1 ? 1 : -1) * st3[t >> 1]];
+          w[t] = rr.d[t >> 1];
+          ln[t] = rr.lam;
+        }
+      }
+      T gs = T(0);
+      if (mt & CODE_SEED) {
+        if constexpr (sizeof(T) == 4)
+          gs = A.gdense ? A.gdense[sd.u_off + x] : seed_lookup(sidx, sval, ns, (int64_t)x);
+        else
+          gs = seed_lookup(sidx, sval, ns, (int64_t)x);
+      }
+      rec[x].lam = causal_lambda<T>(mt, dc, w, ln, gs);
+      // release the upwind neighbours (their outstanding bit for this cell)
+      uint32_t rel = 0;
+      int np = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const uint32_t side = (mt >> (2 * a)) & 3u;
+        if (side) {
+          const int tq = x + (side == 1 ? -st3[a] : st3[a]);
+          const uint32_t bit = side == 1 ? (2u << (2 * a)) : (1u << (2 * a));
+          const uint32_t old = atom_and_acq_rel_cta(meta + tq, ~(bit << META_OUT));
+          const uint32_t ob = (old >> META_OUT) & 0x3fu;
+          if ((ob & bit) && !(ob & ~bit)) {
+            rel |= 1u << a;
+            ++np;
+          }
+        }
+      }
+      int pos = take_slots(np, &S.tail);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        if ((rel >> a) & 1u) {
+          const uint32_t side = (mt >> (2 * a)) & 3u;
+          st_release_cta(queue + pos++, x + (side == 1 ? -st3[a] : st3[a]));
+        }
     }
+    __syncthreads();
     if (A.gdense)  // leave the dense seed field all zero for the next evaluation
       for (int e = tid; e < ns; e += nth) A.gdense[sd.u_off + sidx[e]] = T(0);
     if (tid == 0) {
       adt_solve_status& st = A.status[sd.gidx];
-      st.adj_iters = r;  // rounds
-      st.adj_converged = base == S.nonfixed ? 1 : 0;  // else the users graph had a cycle
-      upd += (unsigned long long)base;
+      st.adj_iters = 1;
+      // every non-fixed cell queued and evaluated, no wait ran out
+      st.adj_converged = (S.err == 0 && S.tail == S.nonfixed && S.head >= S.nonfixed) ? 1 : 0;
+      upd += (unsigned long long)S.tail;
       S.q = atomicAdd(A.next, 1) + (int)gridDim.x;
     }
     __syncthreads();

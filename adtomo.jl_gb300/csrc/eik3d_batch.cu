@@ -106,9 +106,6 @@ struct KernelSet {
   const void* grad;
 };
 
-// Queue entries per thread per pass of the causal-order adjoint.
-constexpr int CAUSAL_NB = 2;
-
 template <class T>
 static KernelSet kernels_for(int bk) {
   constexpr int MODE = sizeof(T) == 8 ? MODE_EXACT : MODE_STABLE;
@@ -123,7 +120,7 @@ static KernelSet kernels_for(int bk) {
     k.fwd = (const void*)&k_batch_fwd<T, 32, MODE>;
     k.adj = (const void*)&k_batch_adj<T, 32>;
   }
-  k.adj_causal = (const void*)&k_batch_adj_causal<T, CAUSAL_NB>;
+  k.adj_causal = (const void*)&k_batch_adj_causal<T>;
   k.misfit = (const void*)&k_batch_misfit<T>;
   k.grad = (const void*)&k_batch_grad<T>;
   return k;

@@ -45,8 +45,8 @@ typedef struct adt_solve_status {
   int32_t iters;     /* forward iterations (one iteration = all orderings) */
   int32_t converged; /* 1 if the stopping rule was met before the iteration cap */
   double final_err;  /* last stopping-rule value */
-  int32_t adj_iters; /* adjoint iterations (0 if no adjoint ran); rounds of released
-                        cells for the causal-order adjoint (adt_batch_opts.adj_solver) */
+  int32_t adj_iters; /* adjoint iterations (0 if no adjoint ran); 1 for the causal-order
+                        adjoint, which evaluates every cell once (adt_batch_opts.adj_solver) */
   int32_t adj_converged;
 } adt_solve_status;
 
