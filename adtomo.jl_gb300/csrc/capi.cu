@@ -254,7 +254,7 @@ int adt_eikonal_three_d_grad_device(const double* grad_u, const double* u, const
   rc = eik3d_single_adjoint(grad_u, u, u0, f, h, (int)m, (int)n, (int)l, 100000, grad_u0, grad_f, &iters,
                             &conv, (cudaStream_t)stream);
   if (rc) return rc;
-  if (!conv) return set_error(ADT_ENOCONV, "eikonal3d_grad: adjoint sweeps did not settle");
+  if (!conv) return set_error(ADT_ENOCONV, "eikonal3d_grad: the adjoint solve did not complete");
   return ADT_OK;
 }
 

@@ -273,6 +273,156 @@ __device__ __forceinline__ T causal_lambda(uint32_t mt, const T (&dc)[3], const 
   }
 }
 
+// Pass 1 over one solve's cells (any precision and depth): upwind sides,
+// fixed flag (u == u0_of(x, i, j, k) or no active axis), upwind
+// differences, lambda = 0 and empty queue slots.
+template <class T, class U0>
+__device__ __forceinline__ void causal_pass1(const T* __restrict__ u, const Geom& g,
+                                             unsigned long long div_nl, unsigned long long div_l,
+                                             uint32_t* meta, CausalRec<T>* rec, int* queue, U0 u0_of,
+                                             int tid, int nth) {
+  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+  const T INF = inf_value<T>();
+  for (int x = tid; x < (int)g.ncell; x += nth) {
+    int i, j, k;
+    cell_ijk((uint32_t)x, g, div_nl, div_l, i, j, k);
+    const T uc = u[x];
+    const T un[6] = {i > 0 ? u[x - sI] : INF, i < g.m - 1 ? u[x + sI] : INF,
+                     j > 0 ? u[x - sJ] : INF, j < g.n - 1 ? u[x + sJ] : INF,
+                     k > 0 ? u[x - 1] : INF, k < g.l - 1 ? u[x + 1] : INF};
+    uint32_t cd = 0;
+    CausalRec<T> rc;
+    rc.lam = T(0);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      uint32_t side;
+      axis_side(uc, un[2 * ax], un[2 * ax + 1], side, rc.d[ax]);
+      cd |= side << (2 * ax);
+    }
+    if (uc == u0_of(x, i, j, k) || cd == 0) cd = CODE_FIXED;
+    meta[x] = cd;
+    rec[x] = rc;
+    queue[x] = -1;
+  }
+}
+
+// Pass 2 over one solve's cells: user bits (and as outstanding bits) from
+// the neighbours' meta words, and the cells without users appended to the
+// queue (counted in *tail).  Every thread of the CTA calls it (warp-uniform
+// loop); returns the thread's count of non-fixed cells.
+__device__ __forceinline__ int causal_pass2(const Geom& g, unsigned long long div_nl,
+                                            unsigned long long div_l, uint32_t* meta, int* queue,
+                                            int* tail, int lane, int warp, int nth) {
+  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+  const int ncell = (int)g.ncell;
+  int nf = 0;
+  for (int x0 = warp * 32; x0 < ncell; x0 += nth) {
+    const int x = x0 + lane;
+    uint32_t by = REM_FIXED;
+    if (x < ncell) {
+      int i, j, k;
+      cell_ijk((uint32_t)x, g, div_nl, div_l, i, j, k);
+      const uint32_t cd = meta[x];
+      if (!(cd & CODE_FIXED)) {
+        auto uses = [&](int64_t r, int ax, uint32_t want) -> bool {
+          const uint32_t cr = meta[r];
+          return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
+        };
+        uint32_t us = 0;
+        if (i > 0 && uses(x - sI, 0, 2u)) us |= 1u;
+        if (i < g.m - 1 && uses(x + sI, 0, 1u)) us |= 2u;
+        if (j > 0 && uses(x - sJ, 1, 2u)) us |= 4u;
+        if (j < g.n - 1 && uses(x + sJ, 1, 1u)) us |= 8u;
+        if (k > 0 && uses(x - 1, 2, 2u)) us |= 16u;
+        if (k < g.l - 1 && uses(x + 1, 2, 1u)) us |= 32u;
+        // only the high bits change (see p2_causal)
+        meta[x] = cd | (us << CODE_USERS) | (us << META_OUT);
+        by = us;
+      }
+    }
+    nf += by != REM_FIXED;
+    const int pos = warp_append(by == 0u ? 1 : 0, tail, lane);
+    if (by == 0u) queue[pos] = x;
+  }
+  return nf;
+}
+
+// The evaluation in causal order (every thread of the CTA): take the next
+// queue slot, wait for its cell, evaluate it from its record and its users'
+// records, release its upwind neighbours and queue the ones released.
+// seed_of(x, meta word) gives the cell's seed value.  Ends when every
+// non-fixed cell has been taken (S.nonfixed) or a wait ran out (S.err).
+template <class T, class Seed>
+__device__ __forceinline__ void causal_evaluate(CausalShared& S, const Geom& g, uint32_t* meta,
+                                                CausalRec<T>* rec, int* queue, Seed seed_of) {
+  const int st3[3] = {g.n * g.l, g.l, 1};
+  const int nonfixed = S.nonfixed;
+  for (;;) {
+    const int slot = take_slots(1, &S.head);
+    if (slot >= nonfixed) break;
+    int x = ld_acquire_cta(queue + slot);
+    if (x < 0) {
+      const long long t0 = clock64();
+      do {
+        __nanosleep(64);
+        x = ld_acquire_cta(queue + slot);
+      } while (x < 0 && clock64() - t0 < CAUSAL_WAIT_CYCLES &&
+               !*reinterpret_cast<volatile int*>(&S.err));
+      if (x < 0) {  // out of budget, or another thread's was
+        atomicOr(&S.err, 1);
+        break;
+      }
+    }
+    const uint32_t mt = meta[x];
+    const CausalRec<T> rc = rec[x];
+    const T dc[3] = {rc.d[0], rc.d[1], rc.d[2]};
+    // the users' records: adjoint value (final) and upwind difference
+    // towards this cell (its weight)
+    T w[6], ln[6];
+    const uint32_t us = mt >> CODE_USERS;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      w[t] = T(0);
+      ln[t] = T(0);
+      if ((us >> t) & 1u) {
+        const CausalRec<T> rr = rec[x + (t & 1 ? 1 : -1) * st3[t >> 1]];
+        w[t] = rr.d[t >> 1];
+        ln[t] = rr.lam;
+      }
+    }
+    rec[x].lam = causal_lambda<T>(mt, dc, w, ln, seed_of(x, mt));
+    // release the upwind neighbours (their outstanding bit for this cell)
+    uint32_t rel = 0;
+    int np = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const uint32_t side = (mt >> (2 * a)) & 3u;
+      if (side) {
+        const int tq = x + (side == 1 ? -st3[a] : st3[a]);
+        const uint32_t bit = side == 1 ? (2u << (2 * a)) : (1u << (2 * a));
+        const uint32_t old = atom_and_acq_rel_cta(meta + tq, ~(bit << META_OUT));
+        const uint32_t ob = (old >> META_OUT) & 0x3fu;
+        if ((ob & bit) && !(ob & ~bit)) {
+          rel |= 1u << a;
+          ++np;
+        }
+      }
+    }
+    int pos = take_slots(np, &S.tail);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      if ((rel >> a) & 1u) {
+        const uint32_t side = (mt >> (2 * a)) & 3u;
+        st_release_cta(queue + pos++, x + (side == 1 ? -st3[a] : st3[a]));
+      }
+  }
+}
+
+// Every non-fixed cell queued and evaluated, and no wait ran out.
+__device__ __forceinline__ bool causal_complete(const CausalShared& S) {
+  return S.err == 0 && S.tail == S.nonfixed && S.head >= S.nonfixed;
+}
+
 template <class T>
 __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
   __shared__ CausalShared S;
@@ -288,10 +438,8 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     uint32_t* meta = A.meta32 + sd.u_off;
     CausalRec<T>* rec = A.rec + sd.u_off;
     int* queue = A.queue + sd.u_off;
-    const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
     const int ncell = (int)g.ncell;
     const bool vec4 = sizeof(T) == 4 && (g.l % 4) == 0;
-    const T INF = inf_value<T>();
     if (tid == 0) {
       S.head = S.tail = 0;
       S.nonfixed = 0;
@@ -309,27 +457,8 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
         }
     }
     if (!vec4)
-      for (int x = tid; x < ncell; x += nth) {
-        int i, j, k;
-        cell_ijk((uint32_t)x, g, fd.div_nl, fd.div_l, i, j, k);
-        const T uc = u[x];
-        const T un[6] = {i > 0 ? u[x - sI] : INF, i < g.m - 1 ? u[x + sI] : INF,
-                         j > 0 ? u[x - sJ] : INF, j < g.n - 1 ? u[x + sJ] : INF,
-                         k > 0 ? u[x - 1] : INF, k < g.l - 1 ? u[x + 1] : INF};
-        uint32_t cd = 0;
-        CausalRec<T> rc;
-        rc.lam = T(0);
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-          uint32_t side;
-          axis_side(uc, un[2 * ax], un[2 * ax + 1], side, rc.d[ax]);
-          cd |= side << (2 * ax);
-        }
-        if (uc == u0_t<T>(sd, i, j, k) || cd == 0) cd = CODE_FIXED;
-        meta[x] = cd;
-        rec[x] = rc;
-        queue[x] = -1;
-      }
+      causal_pass1<T>(u, g, fd.div_nl, fd.div_l, meta, rec, queue,
+                      [&](int, int i, int j, int k) { return u0_t<T>(sd, i, j, k); }, tid, nth);
     __syncthreads();
     // pass 2: user bits and frontier 0 (the cells nobody uses).  Warp-uniform
     // loops (warp_append needs all lanes).
@@ -356,34 +485,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
           if (((bytes >> (8 * b)) & 0xffu) == 0u) queue[pos++] = 4 * e + b;
       }
     } else {
-      for (int x0 = warp * 32; x0 < ncell; x0 += nth) {
-        const int x = x0 + lane;
-        uint32_t by = REM_FIXED;
-        if (x < ncell) {
-          int i, j, k;
-          cell_ijk((uint32_t)x, g, fd.div_nl, fd.div_l, i, j, k);
-          const uint32_t cd = meta[x];
-          if (!(cd & CODE_FIXED)) {
-            auto uses = [&](int64_t r, int ax, uint32_t want) -> bool {
-              const uint32_t cr = meta[r];
-              return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
-            };
-            uint32_t us = 0;
-            if (i > 0 && uses(x - sI, 0, 2u)) us |= 1u;
-            if (i < g.m - 1 && uses(x + sI, 0, 1u)) us |= 2u;
-            if (j > 0 && uses(x - sJ, 1, 2u)) us |= 4u;
-            if (j < g.n - 1 && uses(x + sJ, 1, 1u)) us |= 8u;
-            if (k > 0 && uses(x - 1, 2, 2u)) us |= 16u;
-            if (k < g.l - 1 && uses(x + 1, 2, 1u)) us |= 32u;
-            // only the high bits change (see p2_causal)
-            meta[x] = cd | (us << CODE_USERS) | (us << META_OUT);
-            by = us;
-          }
-        }
-        nf += by != REM_FIXED;
-        const int pos = warp_append(by == 0u ? 1 : 0, &S.tail, lane);
-        if (by == 0u) queue[pos] = x;
-      }
+      nf = causal_pass2(g, fd.div_nl, fd.div_l, meta, queue, &S.tail, lane, warp, nth);
     }
     nf = __reduce_add_sync(0xffffffffu, nf);
     if (lane == 0 && nf) atomicAdd(&S.nonfixed, nf);
@@ -399,74 +501,13 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     }
     __syncthreads();
     // evaluation in causal order
-    const int st3[3] = {(int)sI, (int)sJ, 1};
-    const int nonfixed = S.nonfixed;
-    for (;;) {
-      const int slot = take_slots(1, &S.head);
-      if (slot >= nonfixed) break;
-      int x = ld_acquire_cta(queue + slot);
-      if (x < 0) {
-        const long long t0 = clock64();
-        do {
-          __nanosleep(64);
-          x = ld_acquire_cta(queue + slot);
-        } while (x < 0 && clock64() - t0 < CAUSAL_WAIT_CYCLES &&
-                 !*reinterpret_cast<volatile int*>(&S.err));
-        if (x < 0) {  // out of budget, or another thread's was
-          atomicOr(&S.err, 1);
-          break;
-        }
-      }
-      const uint32_t mt = meta[x];
-      const CausalRec<T> rc = rec[x];
-      const T dc[3] = {rc.d[0], rc.d[1], rc.d[2]};
-      // the users' records: adjoint value (final) and upwind difference
-      // towards this cell (its weight)
-      T w[6], ln[6];
-      const uint32_t us = mt >> CODE_USERS;
-#pragma unroll
-      for (int t = 0; t < 6; ++t) {
-        w[t] = T(0);
-        ln[t] = T(0);
-        if ((us >> t) & 1u) {
-          const CausalRec<T> rr = rec[x + (t & 1 ? 1 : -1) * st3[t >> 1]];
-          w[t] = rr.d[t >> 1];
-          ln[t] = rr.lam;
-        }
-      }
-      T gs = T(0);
-      if (mt & CODE_SEED) {
-        if constexpr (sizeof(T) == 4)
-          gs = A.gdense ? A.gdense[sd.u_off + x] : seed_lookup(sidx, sval, ns, (int64_t)x);
-        else
-          gs = seed_lookup(sidx, sval, ns, (int64_t)x);
-      }
-      rec[x].lam = causal_lambda<T>(mt, dc, w, ln, gs);
-      // release the upwind neighbours (their outstanding bit for this cell)
-      uint32_t rel = 0;
-      int np = 0;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const uint32_t side = (mt >> (2 * a)) & 3u;
-        if (side) {
-          const int tq = x + (side == 1 ? -st3[a] : st3[a]);
-          const uint32_t bit = side == 1 ? (2u << (2 * a)) : (1u << (2 * a));
-          const uint32_t old = atom_and_acq_rel_cta(meta + tq, ~(bit << META_OUT));
-          const uint32_t ob = (old >> META_OUT) & 0x3fu;
-          if ((ob & bit) && !(ob & ~bit)) {
-            rel |= 1u << a;
-            ++np;
-          }
-        }
-      }
-      int pos = take_slots(np, &S.tail);
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        if ((rel >> a) & 1u) {
-          const uint32_t side = (mt >> (2 * a)) & 3u;
-          st_release_cta(queue + pos++, x + (side == 1 ? -st3[a] : st3[a]));
-        }
-    }
+    causal_evaluate<T>(S, g, meta, rec, queue, [&](int x, uint32_t mt) -> T {
+      if (!(mt & CODE_SEED)) return T(0);
+      if constexpr (sizeof(T) == 4)
+        return A.gdense ? A.gdense[sd.u_off + x] : seed_lookup(sidx, sval, ns, (int64_t)x);
+      else
+        return seed_lookup(sidx, sval, ns, (int64_t)x);
+    });
     __syncthreads();
     if (A.gdense)  // leave the dense seed field all zero for the next evaluation
       for (int e = tid; e < ns; e += nth) A.gdense[sd.u_off + sidx[e]] = T(0);
@@ -474,7 +515,7 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
       adt_solve_status& st = A.status[sd.gidx];
       st.adj_iters = 1;
       // every non-fixed cell queued and evaluated, no wait ran out
-      st.adj_converged = (S.err == 0 && S.tail == S.nonfixed && S.head >= S.nonfixed) ? 1 : 0;
+      st.adj_converged = causal_complete(S) ? 1 : 0;
       upd += (unsigned long long)S.tail;
       S.q = atomicAdd(A.next, 1) + (int)gridDim.x;
     }
@@ -483,6 +524,35 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     __syncthreads();  // S.q read by all before the next solve's tid 0 writes S
   }
   if (tid == 0 && upd) atomicAdd(&A.counters[2], upd);
+}
+
+// The single-event adjoint (EikonalThreeDGrad, Eikonal3D.cpp:96-198) in
+// causal order, one CTA: u0 is the op's explicit array (fixed cells: u ==
+// u0 or no active axis) and every non-fixed cell starts from its grad_u
+// value, as the oracle's substitution does, so lambda is the oracle's bit
+// for bit.  *complete = 1 when every non-fixed cell was evaluated.
+__global__ void __launch_bounds__(ADT_CAUSAL_MAXT / 2)
+    k_single_adj_causal(const double* __restrict__ u, const double* __restrict__ u0,
+                        const double* __restrict__ grad_u, Geom g, unsigned long long div_nl,
+                        unsigned long long div_l, uint32_t* meta, CausalRec<double>* rec, int* queue,
+                        int* complete) {
+  __shared__ CausalShared S;
+  const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    S.head = S.tail = 0;
+    S.nonfixed = 0;
+    S.err = 0;
+  }
+  causal_pass1<double>(u, g, div_nl, div_l, meta, rec, queue,
+                       [&](int x, int, int, int) { return u0[x]; }, tid, nth);
+  __syncthreads();
+  int nf = causal_pass2(g, div_nl, div_l, meta, queue, &S.tail, lane, warp, nth);
+  nf = __reduce_add_sync(0xffffffffu, nf);
+  if (lane == 0 && nf) atomicAdd(&S.nonfixed, nf);
+  __syncthreads();
+  causal_evaluate<double>(S, g, meta, rec, queue, [&](int x, uint32_t) { return grad_u[x]; });
+  __syncthreads();
+  if (tid == 0) *complete = causal_complete(S) ? 1 : 0;
 }
 
 }  // namespace adt

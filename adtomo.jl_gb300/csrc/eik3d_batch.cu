@@ -932,6 +932,23 @@ int batch_stats(BatchPlan* P, adt_batch_stats* s) {
 
 void* batch_stream(BatchPlan* P) { return (void*)P->stream; }
 
+static_assert(sizeof(CausalRec<double>) == CAUSAL_REC64_BYTES, "record size");
+
+int causal_single_adjoint(const double* d_u, const double* d_u0, const double* d_grad_u, int m,
+                          int n, int l, uint32_t* meta, void* rec, int* queue, int* d_complete,
+                          void* stream) {
+  const Geom g = make_geom(m, n, l, SBK);
+  FieldDev<double> fd;
+  std::memset(&fd, 0, sizeof fd);
+  fd.g = g;
+  set_divisors(fd);
+  k_single_adj_causal<<<1, ADT_CAUSAL_MAXT / 2, 0, (cudaStream_t)stream>>>(
+      d_u, d_u0, d_grad_u, g, fd.div_nl, fd.div_l, meta, static_cast<CausalRec<double>*>(rec), queue,
+      d_complete);
+  ADT_CUDA(cudaGetLastError());
+  return ADT_OK;
+}
+
 void* batch_device_buffer(BatchPlan* P, int which) {
   switch (which) {
     case 0: return P->d_slow64.p;

@@ -1,5 +1,7 @@
 // eik3d_batch.h -- batched misfit + gradient plan (host side).
 #pragma once
+#include <cstddef>
+#include <cstdint>
 #include "../../include/adtomo_gpu.h"
 
 namespace adt {
@@ -24,5 +26,14 @@ int batch_download(BatchPlan* p, double* misfit, double* t_pred, double* grad,
 int batch_stats(BatchPlan* p, adt_batch_stats* s);
 void* batch_stream(BatchPlan* p);
 void* batch_device_buffer(BatchPlan* p, int which);
+
+// The single-event 3D adjoint in causal order (k_single_adj_causal), for
+// grids of fewer than 2^31 cells: lambda into rec (ncell records of
+// CAUSAL_REC64_BYTES bytes, lambda first), *d_complete = 1 when every
+// non-fixed cell was evaluated.  meta and queue: ncell words each.
+constexpr size_t CAUSAL_REC64_BYTES = 32;
+int causal_single_adjoint(const double* d_u, const double* d_u0, const double* d_grad_u, int m,
+                          int n, int l, uint32_t* meta, void* rec, int* queue, int* d_complete,
+                          void* stream);
 
 }  // namespace adt

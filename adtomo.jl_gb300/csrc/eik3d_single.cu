@@ -14,6 +14,7 @@
 #include <mutex>
 
 #include "eik3d_brick.cuh"
+#include "eik3d_batch.h"
 #include "eik3d_common_host.h"
 #include "eik3d_single.h"
 #include "eik3d_single_kernels.h"
@@ -166,7 +167,9 @@ __global__ void k_level_adj(const double* __restrict__ u, double* __restrict__ l
   }
 }
 
-__global__ void k_grad(const double* __restrict__ lam, const double* __restrict__ f,
+// lambda of cell c is lam[c * lam_stride]: 1 for the sweeps' array, 4 for the
+// causal-order adjoint's records.
+__global__ void k_grad(const double* __restrict__ lam, int lam_stride, const double* __restrict__ f,
                        const double* __restrict__ u, const double* __restrict__ u0,
                        const double* __restrict__ gu, double h, int64_t n,
                        double* __restrict__ grad_f, double* __restrict__ grad_u0) {
@@ -174,7 +177,7 @@ __global__ void k_grad(const double* __restrict__ lam, const double* __restrict_
        c += (int64_t)gridDim.x * blockDim.x) {
     // rhs = -2 f h h ; grad_f = -lambda * rhs  (Eikonal3D.cpp:163-166,244-246)
     const double rhs = __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f[c]), h), h);
-    grad_f[c] = __dmul_rn(-lam[c], rhs);
+    grad_f[c] = __dmul_rn(-lam[c * lam_stride], rhs);
     if (grad_u0) grad_u0[c] = (u[c] == u0[c]) ? gu[c] : 0.0;
   }
 }
@@ -183,6 +186,7 @@ namespace {
 struct SingleWork {
   std::mutex mu;
   DevBuf uold, lam, code1, code, levels, scalar;
+  DevBuf meta, rec, queue;  // causal-order adjoint
   int lev_m = -1, lev_n = -1, lev_l = -1;
   LevelList host_levels;
 };
@@ -278,6 +282,30 @@ int eik3d_single_adjoint(const double* d_gu, const double* d_u, const double* d_
   SingleWork& W = work(dev);
   std::lock_guard<std::mutex> lock(W.mu);
   const Geom g = make_geom(m, n, l, SBK);
+  if (g.ncell < ((int64_t)1 << 31)) {
+    // causal order: every cell evaluated once, after its users, in one CTA
+    // (the same per-cell formula as the sweeps below, so the same bits)
+    ADT_CUDA(W.scalar.reserve(sizeof(unsigned long long)));
+    ADT_CUDA(W.meta.reserve((size_t)g.ncell * sizeof(uint32_t)));
+    ADT_CUDA(W.rec.reserve((size_t)g.ncell * CAUSAL_REC64_BYTES));
+    ADT_CUDA(W.queue.reserve((size_t)g.ncell * sizeof(int)));
+    int* d_complete = W.scalar.as<int>();
+    int rc;
+    if ((rc = causal_single_adjoint(d_u, d_u0, d_gu, m, n, l, W.meta.as<uint32_t>(), W.rec.p,
+                                    W.queue.as<int>(), d_complete, stream)))
+      return rc;
+    k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(W.rec.as<double>(),
+                                                  (int)(CAUSAL_REC64_BYTES / sizeof(double)), d_f,
+                                                  d_u, d_u0, d_gu, h, g.ncell, d_gf, d_gu0);
+    ADT_CUDA(cudaGetLastError());
+    int complete = 0;
+    ADT_CUDA(cudaMemcpyAsync(&complete, d_complete, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    ADT_CUDA(cudaStreamSynchronize(stream));
+    if (iters_out) *iters_out = 1;
+    if (converged_out) *converged_out = complete;
+    return ADT_OK;
+  }
+  // larger grids: reverse level sweeps until nothing changes
   int rc = ensure_levels(W, g, stream);
   if (rc) return rc;
   ADT_CUDA(W.lam.reserve((size_t)g.ncell * sizeof(double)));
@@ -320,7 +348,7 @@ int eik3d_single_adjoint(const double* d_gu, const double* d_u, const double* d_
       break;
     }
   }
-  k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(lam, d_f, d_u, d_u0, d_gu, h, g.ncell, d_gf, d_gu0);
+  k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(lam, 1, d_f, d_u, d_u0, d_gu, h, g.ncell, d_gf, d_gu0);
   ADT_CUDA(cudaGetLastError());
   ADT_CUDA(cudaStreamSynchronize(stream));
   if (iters_out) *iters_out = done ? it + 1 : it;
