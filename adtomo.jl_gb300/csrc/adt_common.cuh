@@ -116,4 +116,48 @@ inline Geom make_geom(int m, int n, int l, int BK) {
   return g;
 }
 
+// Blocked cell layout of the causal-order adjoint's per-cell words and
+// records: groups of 2 x 2 x 2 cells stored together (eight 16-byte FP32
+// records fill one 128-byte line), groups in (i, j, k) order.  A cell's
+// neighbour along an axis lies in its own group when the coordinate's low
+// bit allows and in the adjacent group otherwise, so half of a cell's
+// neighbourhood shares its line.  Grids with odd extents leave the unused
+// slots of their last groups untouched (no in-grid cell refers to them).
+struct BlkMap {
+  int nj2, nk2;  // groups along j and k
+  int gi;        // slots per group step along i: nj2 * nk2 * 8
+};
+__host__ __device__ inline BlkMap make_blkmap(int n, int l) {
+  BlkMap b;
+  b.nj2 = (n + 1) / 2;
+  b.nk2 = (l + 1) / 2;
+  b.gi = b.nj2 * b.nk2 * 8;
+  return b;
+}
+// Slots of one solve in the blocked layout (< 2^31 where it is used).
+__host__ __device__ inline int64_t blk_slots(int m, int n, int l) {
+  return (int64_t)((m + 1) / 2) * ((n + 1) / 2) * ((l + 1) / 2) * 8;
+}
+__host__ __device__ __forceinline__ int blk_index(const BlkMap& b, int i, int j, int k) {
+  return ((i >> 1) * b.nj2 + (j >> 1)) * b.nk2 * 8 + (k >> 1) * 8 +
+         (((i & 1) << 2) | ((j & 1) << 1) | (k & 1));
+}
+// The slot of the neighbour of slot s along axis a (0: i, 1: j, 2: k) in
+// direction +1 (dir > 0) or -1; the caller knows that neighbour is in the grid.
+__host__ __device__ __forceinline__ int blk_step(const BlkMap& b, int s, int a, int dir) {
+  const int bit = 4 >> a;
+  const int gs = a == 0 ? b.gi : (a == 1 ? b.nk2 * 8 : 8);
+  if (dir > 0) return (s & bit) ? s - bit + gs : s + bit;
+  return (s & bit) ? s - bit : s + bit - gs;
+}
+// (i, j, k) of slot s (plain divisions: used for the few seeded cells).
+__host__ __device__ __forceinline__ void blk_cell(const BlkMap& b, int s, int& i, int& j, int& k) {
+  const int g = s >> 3, w = s & 7;
+  const int gjk = b.nj2 * b.nk2;
+  const int I = g / gjk, r = g - I * gjk, J = r / b.nk2, K = r - J * b.nk2;
+  i = 2 * I + (w >> 2);
+  j = 2 * J + ((w >> 1) & 1);
+  k = 2 * K + (w & 1);
+}
+
 }  // namespace adt

@@ -13,7 +13,9 @@
 // One CTA runs one solve at a time (solves from the chunk's work counter).
 // Per cell the kernel keeps a 32-bit meta word (upwind sides, fixed, seed,
 // user bits, and the user bits still outstanding in bits 16-21) and a record
-// {lambda, upwind difference per axis} (CausalRec):
+// {lambda, upwind difference per axis} (CausalRec), both in the blocked
+// layout of 2 x 2 x 2 cell groups (BlkMap), which keeps most of a cell's
+// neighbourhood in its own 128-byte line:
 //  - pass 1 reads the travel times once (coalesced) and writes the sides,
 //    the fixed flag and the differences; pass 2 the user bits, from the
 //    neighbours' meta words;
@@ -166,78 +168,6 @@ __device__ __forceinline__ void axis_side(T uc, T um, T up, uint32_t& side, T& d
     d = uc > a ? __dsub_rn(uc, a) : 0.0;
 }
 
-// Pass 1 for four consecutive cells (FP32, l % 4 == 0) from p1_load's loads.
-__device__ __forceinline__ void p1_store_causal(const P1Loads& r, uint32_t* meta,
-                                                CausalRec<float>* rec, const SolveDev& sd,
-                                                int64_t x, int i, int j, int k) {
-  const float uc[4] = {r.c4.x, r.c4.y, r.c4.z, r.c4.w};
-  const float vxm[4] = {r.xm.x, r.xm.y, r.xm.z, r.xm.w}, vxp[4] = {r.xp.x, r.xp.y, r.xp.z, r.xp.w};
-  const float vym[4] = {r.ym.x, r.ym.y, r.ym.z, r.ym.w}, vyp[4] = {r.yp.x, r.yp.y, r.yp.z, r.yp.w};
-  uint32_t m[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const float um[3] = {vxm[q], vym[q], q == 0 ? r.zm : uc[q - 1]};
-    const float up[3] = {vxp[q], vyp[q], q == 3 ? r.zp : uc[q + 1]};
-    uint32_t cd = 0;
-    CausalRec<float> rc;
-    rc.lam = 0.0f;
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      uint32_t side;
-      axis_side(uc[q], um[ax], up[ax], side, rc.d[ax]);
-      cd |= side << (2 * ax);
-    }
-    if (uc[q] == u0_t<float>(sd, i, j, k + q) || cd == 0) cd = CODE_FIXED;
-    m[q] = cd;
-    rec[x + q] = rc;
-  }
-  *reinterpret_cast<uint4*>(meta + x) = make_uint4(m[0], m[1], m[2], m[3]);
-}
-
-// Pass 2 for four consecutive cells from 16-byte loads of the meta words:
-// user bits (neighbour r uses c when r is not fixed and its side along the
-// axis points at c), written to bits 8-13 and, as outstanding, 16-21.
-// Returns one byte per cell: its user bits, or REM_FIXED for a fixed cell.
-__device__ __forceinline__ uint32_t p2_causal(uint32_t* meta, const Geom& g, int64_t x, int i, int j,
-                                              int k) {
-  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
-  auto ld4 = [&](int64_t y) -> uint4 { return *reinterpret_cast<const uint4*>(meta + y); };
-  const uint4 fixed4 = make_uint4(CODE_FIXED, CODE_FIXED, CODE_FIXED, CODE_FIXED);
-  const uint4 c4 = ld4(x);
-  const uint4 xm = i > 0 ? ld4(x - sI) : fixed4, xp = i < g.m - 1 ? ld4(x + sI) : fixed4;
-  const uint4 ym = j > 0 ? ld4(x - sJ) : fixed4, yp = j < g.n - 1 ? ld4(x + sJ) : fixed4;
-  const uint32_t zm = k > 0 ? meta[x - 1] : CODE_FIXED, zp = k + 4 < g.l ? meta[x + 4] : CODE_FIXED;
-  const uint32_t cc[4] = {c4.x, c4.y, c4.z, c4.w};
-  const uint32_t vxm[4] = {xm.x, xm.y, xm.z, xm.w}, vxp[4] = {xp.x, xp.y, xp.z, xp.w};
-  const uint32_t vym[4] = {ym.x, ym.y, ym.z, ym.w}, vyp[4] = {yp.x, yp.y, yp.z, yp.w};
-  auto uses = [](uint32_t cr, int ax, uint32_t want) -> bool {
-    return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
-  };
-  uint32_t out[4], bytes = 0;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    uint32_t cd = cc[q];
-    if (cd & CODE_FIXED) {
-      bytes |= REM_FIXED << (8 * q);
-    } else {
-      uint32_t us = 0;
-      if (uses(vxm[q], 0, 2u)) us |= 1u;
-      if (uses(vxp[q], 0, 1u)) us |= 2u;
-      if (uses(vym[q], 1, 2u)) us |= 4u;
-      if (uses(vyp[q], 1, 1u)) us |= 8u;
-      if (uses(q == 0 ? zm : cc[q - 1], 2, 2u)) us |= 16u;
-      if (uses(q == 3 ? zp : cc[q + 1], 2, 1u)) us |= 32u;
-      cd |= (us << CODE_USERS) | (us << META_OUT);
-      bytes |= us << (8 * q);
-    }
-    out[q] = cd;
-  }
-  // only bits above the sides and the fixed flag change: a neighbour reading
-  // these words concurrently sees the same low bits either way
-  *reinterpret_cast<uint4*>(meta + x) = make_uint4(out[0], out[1], out[2], out[3]);
-  return bytes;
-}
-
 // The adjoint value of one non-fixed cell: meta word mt, its own upwind
 // differences dc, its users' upwind differences towards it (w, 0 for a
 // neighbour that is not a user) and adjoint values (ln, 0 likewise), in the
@@ -273,14 +203,15 @@ __device__ __forceinline__ T causal_lambda(uint32_t mt, const T (&dc)[3], const 
   }
 }
 
-// Pass 1 over one solve's cells (any precision and depth): upwind sides,
-// fixed flag (u == u0_of(x, i, j, k) or no active axis), upwind
-// differences, lambda = 0 and empty queue slots.
+// Pass 1 over one solve's cells: upwind sides, fixed flag (u ==
+// u0_of(x, i, j, k) or no active axis), upwind differences and lambda = 0
+// into the blocked meta words and records, and empty queue slots.  Reads the
+// travel times in their own order (coalesced).
 template <class T, class U0>
 __device__ __forceinline__ void causal_pass1(const T* __restrict__ u, const Geom& g,
                                              unsigned long long div_nl, unsigned long long div_l,
-                                             uint32_t* meta, CausalRec<T>* rec, int* queue, U0 u0_of,
-                                             int tid, int nth) {
+                                             const BlkMap& bm, uint32_t* meta, CausalRec<T>* rec,
+                                             int* queue, U0 u0_of, int tid, int nth) {
   const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
   const T INF = inf_value<T>();
   for (int x = tid; x < (int)g.ncell; x += nth) {
@@ -300,49 +231,53 @@ __device__ __forceinline__ void causal_pass1(const T* __restrict__ u, const Geom
       cd |= side << (2 * ax);
     }
     if (uc == u0_of(x, i, j, k) || cd == 0) cd = CODE_FIXED;
-    meta[x] = cd;
-    rec[x] = rc;
+    const int b = blk_index(bm, i, j, k);
+    meta[b] = cd;
+    rec[b] = rc;
     queue[x] = -1;
   }
 }
 
 // Pass 2 over one solve's cells: user bits (and as outstanding bits) from
 // the neighbours' meta words, and the cells without users appended to the
-// queue (counted in *tail).  Every thread of the CTA calls it (warp-uniform
-// loop); returns the thread's count of non-fixed cells.
+// queue (counted in *tail) by their blocked slots.  Every thread of the CTA
+// calls it (warp-uniform loop); returns the thread's count of non-fixed cells.
 __device__ __forceinline__ int causal_pass2(const Geom& g, unsigned long long div_nl,
-                                            unsigned long long div_l, uint32_t* meta, int* queue,
-                                            int* tail, int lane, int warp, int nth) {
-  const int64_t sI = (int64_t)g.n * g.l, sJ = g.l;
+                                            unsigned long long div_l, const BlkMap& bm,
+                                            uint32_t* meta, int* queue, int* tail, int lane, int warp,
+                                            int nth) {
   const int ncell = (int)g.ncell;
   int nf = 0;
   for (int x0 = warp * 32; x0 < ncell; x0 += nth) {
     const int x = x0 + lane;
     uint32_t by = REM_FIXED;
+    int b = 0;
     if (x < ncell) {
       int i, j, k;
       cell_ijk((uint32_t)x, g, div_nl, div_l, i, j, k);
-      const uint32_t cd = meta[x];
+      b = blk_index(bm, i, j, k);
+      const uint32_t cd = meta[b];
       if (!(cd & CODE_FIXED)) {
-        auto uses = [&](int64_t r, int ax, uint32_t want) -> bool {
-          const uint32_t cr = meta[r];
-          return !(cr & CODE_FIXED) && ((cr >> (2 * ax)) & 3u) == want;
+        auto uses = [&](int a, int dir, uint32_t want) -> bool {
+          const uint32_t cr = meta[blk_step(bm, b, a, dir)];
+          return !(cr & CODE_FIXED) && ((cr >> (2 * a)) & 3u) == want;
         };
         uint32_t us = 0;
-        if (i > 0 && uses(x - sI, 0, 2u)) us |= 1u;
-        if (i < g.m - 1 && uses(x + sI, 0, 1u)) us |= 2u;
-        if (j > 0 && uses(x - sJ, 1, 2u)) us |= 4u;
-        if (j < g.n - 1 && uses(x + sJ, 1, 1u)) us |= 8u;
-        if (k > 0 && uses(x - 1, 2, 2u)) us |= 16u;
-        if (k < g.l - 1 && uses(x + 1, 2, 1u)) us |= 32u;
-        // only the high bits change (see p2_causal)
-        meta[x] = cd | (us << CODE_USERS) | (us << META_OUT);
+        if (i > 0 && uses(0, -1, 2u)) us |= 1u;
+        if (i < g.m - 1 && uses(0, 1, 1u)) us |= 2u;
+        if (j > 0 && uses(1, -1, 2u)) us |= 4u;
+        if (j < g.n - 1 && uses(1, 1, 1u)) us |= 8u;
+        if (k > 0 && uses(2, -1, 2u)) us |= 16u;
+        if (k < g.l - 1 && uses(2, 1, 1u)) us |= 32u;
+        // only the high bits change: a neighbour reading this word
+        // concurrently sees the same side bits either way
+        meta[b] = cd | (us << CODE_USERS) | (us << META_OUT);
         by = us;
       }
     }
     nf += by != REM_FIXED;
     const int pos = warp_append(by == 0u ? 1 : 0, tail, lane);
-    if (by == 0u) queue[pos] = x;
+    if (by == 0u) queue[pos] = b;
   }
   return nf;
 }
@@ -350,12 +285,11 @@ __device__ __forceinline__ int causal_pass2(const Geom& g, unsigned long long di
 // The evaluation in causal order (every thread of the CTA): take the next
 // queue slot, wait for its cell, evaluate it from its record and its users'
 // records, release its upwind neighbours and queue the ones released.
-// seed_of(x, meta word) gives the cell's seed value.  Ends when every
+// Cells are blocked slots; seed_of(slot, meta word) gives the cell's seed value.  Ends when every
 // non-fixed cell has been taken (S.nonfixed) or a wait ran out (S.err).
 template <class T, class Seed>
-__device__ __forceinline__ void causal_evaluate(CausalShared& S, const Geom& g, uint32_t* meta,
+__device__ __forceinline__ void causal_evaluate(CausalShared& S, const BlkMap& bm, uint32_t* meta,
                                                 CausalRec<T>* rec, int* queue, Seed seed_of) {
-  const int st3[3] = {g.n * g.l, g.l, 1};
   const int nonfixed = S.nonfixed;
   for (;;) {
     const int slot = take_slots(1, &S.head);
@@ -385,7 +319,7 @@ __device__ __forceinline__ void causal_evaluate(CausalShared& S, const Geom& g, 
       w[t] = T(0);
       ln[t] = T(0);
       if ((us >> t) & 1u) {
-        const CausalRec<T> rr = rec[x + (t & 1 ? 1 : -1) * st3[t >> 1]];
+        const CausalRec<T> rr = rec[blk_step(bm, x, t >> 1, t & 1 ? 1 : -1)];
         w[t] = rr.d[t >> 1];
         ln[t] = rr.lam;
       }
@@ -398,7 +332,7 @@ __device__ __forceinline__ void causal_evaluate(CausalShared& S, const Geom& g, 
     for (int a = 0; a < 3; ++a) {
       const uint32_t side = (mt >> (2 * a)) & 3u;
       if (side) {
-        const int tq = x + (side == 1 ? -st3[a] : st3[a]);
+        const int tq = blk_step(bm, x, a, side == 1 ? -1 : 1);
         const uint32_t bit = side == 1 ? (2u << (2 * a)) : (1u << (2 * a));
         const uint32_t old = atom_and_acq_rel_cta(meta + tq, ~(bit << META_OUT));
         const uint32_t ob = (old >> META_OUT) & 0x3fu;
@@ -413,7 +347,7 @@ __device__ __forceinline__ void causal_evaluate(CausalShared& S, const Geom& g, 
     for (int a = 0; a < 3; ++a)
       if ((rel >> a) & 1u) {
         const uint32_t side = (mt >> (2 * a)) & 3u;
-        st_release_cta(queue + pos++, x + (side == 1 ? -st3[a] : st3[a]));
+        st_release_cta(queue + pos++, blk_step(bm, x, a, side == 1 ? -1 : 1));
       }
   }
 }
@@ -434,59 +368,22 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     const SolveDev& sd = A.solves[gsol];
     const FieldDev<T> fd = A.fields[sd.field];
     const Geom g = fd.g;
-    const T* __restrict__ u = A.u + sd.u_off;
+    const BlkMap bm = make_blkmap(g.n, g.l);
+    // per-solve regions hold max(cells, blocked slots) (batch_create)
     uint32_t* meta = A.meta32 + sd.u_off;
     CausalRec<T>* rec = A.rec + sd.u_off;
     int* queue = A.queue + sd.u_off;
-    const int ncell = (int)g.ncell;
-    const bool vec4 = sizeof(T) == 4 && (g.l % 4) == 0;
     if (tid == 0) {
       S.head = S.tail = 0;
       S.nonfixed = 0;
       S.err = 0;
     }
     // pass 1: sides, fixed cells, upwind differences; lambda = 0
-    if constexpr (sizeof(T) == 4) {
-      if (vec4)
-        for (int e = tid; e < ncell / 4; e += nth) {
-          int i, j, k;
-          cell_ijk(4u * (uint32_t)e, g, fd.div_nl, fd.div_l, i, j, k);
-          p1_store_causal(p1_load(u, g, 4 * (int64_t)e, i, j, k), meta, rec, sd, 4 * (int64_t)e, i,
-                          j, k);
-          *reinterpret_cast<int4*>(queue + 4 * (int64_t)e) = make_int4(-1, -1, -1, -1);
-        }
-    }
-    if (!vec4)
-      causal_pass1<T>(u, g, fd.div_nl, fd.div_l, meta, rec, queue,
-                      [&](int, int i, int j, int k) { return u0_t<T>(sd, i, j, k); }, tid, nth);
+    causal_pass1<T>(A.u + sd.u_off, g, fd.div_nl, fd.div_l, bm, meta, rec, queue,
+                    [&](int, int i, int j, int k) { return u0_t<T>(sd, i, j, k); }, tid, nth);
     __syncthreads();
-    // pass 2: user bits and frontier 0 (the cells nobody uses).  Warp-uniform
-    // loops (warp_append needs all lanes).
-    int nf = 0;
-    if (vec4) {
-      for (int e0 = warp * 32; e0 < ncell / 4; e0 += nth) {
-        const int e = e0 + lane;
-        uint32_t bytes = 0x80808080u;
-        if (e < ncell / 4) {
-          int i, j, k;
-          cell_ijk(4u * (uint32_t)e, g, fd.div_nl, fd.div_l, i, j, k);
-          bytes = p2_causal(meta, g, 4 * (int64_t)e, i, j, k);
-        }
-        int np = 0;
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const uint32_t by = (bytes >> (8 * b)) & 0xffu;
-          np += by == 0u;
-          nf += by != REM_FIXED;
-        }
-        int pos = warp_append(np, &S.tail, lane);
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-          if (((bytes >> (8 * b)) & 0xffu) == 0u) queue[pos++] = 4 * e + b;
-      }
-    } else {
-      nf = causal_pass2(g, fd.div_nl, fd.div_l, meta, queue, &S.tail, lane, warp, nth);
-    }
+    // pass 2: user bits and the cells nobody uses
+    int nf = causal_pass2(g, fd.div_nl, fd.div_l, bm, meta, queue, &S.tail, lane, warp, nth);
     nf = __reduce_add_sync(0xffffffffu, nf);
     if (lane == 0 && nf) atomicAdd(&S.nonfixed, nf);
     __syncthreads();
@@ -495,18 +392,24 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
     const int64_t* sidx = A.seed_idx + sd.seed_off;
     const T* sval = A.seed_val + sd.seed_off;
     for (int e = tid; e < ns; e += nth) {
-      const int64_t x = sidx[e];
-      const uint32_t cd = meta[x];
-      if (!(cd & CODE_FIXED)) meta[x] = cd | CODE_SEED;
+      int i, j, k;
+      cell_ijk((uint32_t)sidx[e], g, fd.div_nl, fd.div_l, i, j, k);
+      const int b = blk_index(bm, i, j, k);
+      const uint32_t cd = meta[b];
+      if (!(cd & CODE_FIXED)) meta[b] = cd | CODE_SEED;
     }
     __syncthreads();
-    // evaluation in causal order
-    causal_evaluate<T>(S, g, meta, rec, queue, [&](int x, uint32_t mt) -> T {
+    // evaluation in causal order; a seeded cell's value is found by its
+    // position in the solve's own order
+    causal_evaluate<T>(S, bm, meta, rec, queue, [&](int b, uint32_t mt) -> T {
       if (!(mt & CODE_SEED)) return T(0);
+      int i, j, k;
+      blk_cell(bm, b, i, j, k);
+      const int64_t x = ((int64_t)i * g.n + j) * g.l + k;
       if constexpr (sizeof(T) == 4)
-        return A.gdense ? A.gdense[sd.u_off + x] : seed_lookup(sidx, sval, ns, (int64_t)x);
+        return A.gdense ? A.gdense[sd.u_off + x] : seed_lookup(sidx, sval, ns, x);
       else
-        return seed_lookup(sidx, sval, ns, (int64_t)x);
+        return seed_lookup(sidx, sval, ns, x);
     });
     __syncthreads();
     if (A.gdense)  // leave the dense seed field all zero for the next evaluation
@@ -530,7 +433,8 @@ __global__ void ADT_CAUSAL_BOUNDS(T) k_batch_adj_causal(BatchArgs<T> A) {
 // causal order, one CTA: u0 is the op's explicit array (fixed cells: u ==
 // u0 or no active axis) and every non-fixed cell starts from its grad_u
 // value, as the oracle's substitution does, so lambda is the oracle's bit
-// for bit.  *complete = 1 when every non-fixed cell was evaluated.
+// for bit.  meta and rec hold blk_slots(m, n, l) entries (blocked layout),
+// queue one per cell.  *complete = 1 when every non-fixed cell was evaluated.
 __global__ void __launch_bounds__(ADT_CAUSAL_MAXT / 2)
     k_single_adj_causal(const double* __restrict__ u, const double* __restrict__ u0,
                         const double* __restrict__ grad_u, Geom g, unsigned long long div_nl,
@@ -543,14 +447,19 @@ __global__ void __launch_bounds__(ADT_CAUSAL_MAXT / 2)
     S.nonfixed = 0;
     S.err = 0;
   }
-  causal_pass1<double>(u, g, div_nl, div_l, meta, rec, queue,
+  const BlkMap bm = make_blkmap(g.n, g.l);
+  causal_pass1<double>(u, g, div_nl, div_l, bm, meta, rec, queue,
                        [&](int x, int, int, int) { return u0[x]; }, tid, nth);
   __syncthreads();
-  int nf = causal_pass2(g, div_nl, div_l, meta, queue, &S.tail, lane, warp, nth);
+  int nf = causal_pass2(g, div_nl, div_l, bm, meta, queue, &S.tail, lane, warp, nth);
   nf = __reduce_add_sync(0xffffffffu, nf);
   if (lane == 0 && nf) atomicAdd(&S.nonfixed, nf);
   __syncthreads();
-  causal_evaluate<double>(S, g, meta, rec, queue, [&](int x, uint32_t) { return grad_u[x]; });
+  causal_evaluate<double>(S, bm, meta, rec, queue, [&](int b, uint32_t) {
+    int i, j, k;
+    blk_cell(bm, b, i, j, k);
+    return grad_u[((int64_t)i * g.n + j) * g.l + k];
+  });
   __syncthreads();
   if (tid == 0) *complete = causal_complete(S) ? 1 : 0;
 }

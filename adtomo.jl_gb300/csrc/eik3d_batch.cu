@@ -357,7 +357,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
               (o.adj_solver == ADT_ADJ_AUTO && o.precision == ADT_F64);
   if (P->causal)
     for (int f = 0; f < n_fields; ++f)
-      if ((int64_t)dims[3 * f] * dims[3 * f + 1] * dims[3 * f + 2] >= ((int64_t)1 << 31))
+      if (blk_slots(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2]) >= ((int64_t)1 << 31))
         return set_error(ADT_EINVAL, "batch: the causal-order adjoint needs fewer than 2^31 cells "
                          "per field (field %d)", f);
   int64_t sofs = 0;
@@ -434,7 +434,10 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       P->solves[s].meta_off = bricks;
       P->solves[s].seed_off = seeds;
       ch.field_uoff[P->solve_field[s]].push_back(cells);
-      cells += (g.ncell + 15) / 16 * 16;  // 64-byte aligned solves: the FP32 path uses 16-byte accesses
+      // 64-byte aligned solves (the FP32 path uses 16-byte accesses), each
+      // also holding the causal-order adjoint's blocked slots
+      const int64_t span = P->causal ? std::max(g.ncell, blk_slots(g.m, g.n, g.l)) : g.ncell;
+      cells += (span + 15) / 16 * 16;
       bricks += (int64_t)META_ARRAYS_MAX * g.nbx * g.nby * g.nbz;
       seeds += 8LL * P->nsta[P->solve_field[s]];
     }
@@ -738,13 +741,14 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
       // lambda: the sweeps' array, or the causal-order adjoint's records
       const T* lam = P.causal ? P.cb[set].rec.as<T>() : P.cb[set].lam.as<T>();
       int lam_stride = P.causal ? 4 : 1;
+      int bn = P.causal ? P.geoms[f].n : 0, bl = P.causal ? P.geoms[f].l : 0;  // blocked records
       const int64_t* uo = P.d_uoff.as<int64_t>() + ch.dev_uoff_off[f];
       const double* f64 = P.d_slow64.as<double>() + P.cell_off[f];
       double hh = P.h[f];
       int64_t nc = P.geoms[f].ncell;
       double* gr = P.d_grad.as<double>() + P.cell_off[f];
       int cc = cnt;
-      void* args[] = {&lam, &lam_stride, &uo, &cc, &f64, &hh, &nc, &gr};
+      void* args[] = {&lam, &lam_stride, &uo, &cc, &f64, &hh, &nc, &gr, &bn, &bl};
       ADT_CUDA(cudaLaunchKernel(P.ks.grad, dim3(grid1d(nc)), dim3(256), args, 0, st));
     }
     if (P.nsets == 2) ADT_CUDA(cudaEventRecord(P.ev_sync[c + 1], st));

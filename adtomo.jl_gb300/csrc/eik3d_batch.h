@@ -28,9 +28,10 @@ void* batch_stream(BatchPlan* p);
 void* batch_device_buffer(BatchPlan* p, int which);
 
 // The single-event 3D adjoint in causal order (k_single_adj_causal), for
-// grids of fewer than 2^31 cells: lambda into rec (ncell records of
-// CAUSAL_REC64_BYTES bytes, lambda first), *d_complete = 1 when every
-// non-fixed cell was evaluated.  meta and queue: ncell words each.
+// grids of fewer than 2^31 cells: lambda into rec (blk_slots(m, n, l) records
+// of CAUSAL_REC64_BYTES bytes in the blocked layout, lambda first),
+// *d_complete = 1 when every non-fixed cell was evaluated.  meta:
+// blk_slots(m, n, l) words; queue: one word per cell.
 constexpr size_t CAUSAL_REC64_BYTES = 32;
 int causal_single_adjoint(const double* d_u, const double* d_u0, const double* d_grad_u, int m,
                           int n, int l, uint32_t* meta, void* rec, int* queue, int* d_complete,

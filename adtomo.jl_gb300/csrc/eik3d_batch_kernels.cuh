@@ -100,9 +100,9 @@ struct BatchArgs {
   int adj_order_filter;     // 1: adjoint sweeps a brick only in the orderings its flow allows
   int fwd_order_filter;     // 1: FP32 forward sweeps a brick only in the orderings its
                             //    learned upwind directions allow
-  uint32_t* meta32;         // causal-order adjoint: per chunk cell, code bits and outstanding users
-  CausalRec<T>* rec;        // causal-order adjoint: per chunk cell, lambda and upwind differences
-  int* queue;               // causal-order adjoint: frontiers, one int per chunk cell
+  uint32_t* meta32;         // causal-order adjoint: code bits and outstanding users, blocked layout
+  CausalRec<T>* rec;        // causal-order adjoint: lambda and upwind differences, blocked layout
+  int* queue;               // causal-order adjoint: cells in evaluation order, one int per chunk cell
 };
 
 // Per-group scalars at the start of dynamic shared memory.
@@ -1141,10 +1141,19 @@ template <class T>
 __global__ void k_batch_grad(const T* __restrict__ lam, int lam_stride,
                              const int64_t* __restrict__ u_off, int n_solves,
                              const double* __restrict__ f64, double h, int64_t ncell,
-                             double* __restrict__ grad) {
+                             double* __restrict__ grad, int blocked_n, int blocked_l) {
   constexpr int U = 8;
+  const BlkMap bm = make_blkmap(blocked_n, blocked_l);
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
        c += (int64_t)gridDim.x * blockDim.x) {
+    // lc: the cell's slot in lam (blocked_n > 0: the causal-order adjoint's
+    // records in the blocked layout, BlkMap)
+    int64_t lc = c;
+    if (blocked_n > 0) {
+      const int64_t nl = (int64_t)blocked_n * blocked_l;
+      const int i = (int)(c / nl), j = (int)((c - i * nl) / blocked_l);
+      lc = blk_index(bm, i, j, (int)(c - i * nl - (int64_t)j * blocked_l));
+    }
     const double rhs =
         sizeof(T) == 4 ? 0.0 : __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f64[c]), h), h);
     double G = grad[c];
@@ -1152,13 +1161,13 @@ __global__ void k_batch_grad(const T* __restrict__ lam, int lam_stride,
     for (; s + U <= n_solves; s += U) {
       double l[U];
 #pragma unroll
-      for (int q = 0; q < U; ++q) l[q] = (double)lam[(u_off[s + q] + c) * lam_stride];
+      for (int q = 0; q < U; ++q) l[q] = (double)lam[(u_off[s + q] + lc) * lam_stride];
 #pragma unroll
       for (int q = 0; q < U; ++q)
         G = sizeof(T) == 4 ? __dadd_rn(G, -l[q]) : __dadd_rn(G, __dmul_rn(-l[q], rhs));
     }
     for (; s < n_solves; ++s) {
-      const double l = (double)lam[(u_off[s] + c) * lam_stride];
+      const double l = (double)lam[(u_off[s] + lc) * lam_stride];
       G = sizeof(T) == 4 ? __dadd_rn(G, -l) : __dadd_rn(G, __dmul_rn(-l, rhs));
     }
     grad[c] = G;

@@ -167,17 +167,25 @@ __global__ void k_level_adj(const double* __restrict__ u, double* __restrict__ l
   }
 }
 
-// lambda of cell c is lam[c * lam_stride]: 1 for the sweeps' array, 4 for the
-// causal-order adjoint's records.
-__global__ void k_grad(const double* __restrict__ lam, int lam_stride, const double* __restrict__ f,
-                       const double* __restrict__ u, const double* __restrict__ u0,
-                       const double* __restrict__ gu, double h, int64_t n,
-                       double* __restrict__ grad_f, double* __restrict__ grad_u0) {
+// lambda of cell c: lam[c] for the sweeps' array; with blocked_n > 0 the
+// causal-order adjoint's records (4 doubles each, lambda first) in the
+// blocked layout of an m x blocked_n x blocked_l grid.
+__global__ void k_grad(const double* __restrict__ lam, int blocked_n, int blocked_l,
+                       const double* __restrict__ f, const double* __restrict__ u,
+                       const double* __restrict__ u0, const double* __restrict__ gu, double h,
+                       int64_t n, double* __restrict__ grad_f, double* __restrict__ grad_u0) {
+  const BlkMap bm = make_blkmap(blocked_n, blocked_l);
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lc = c;
+    if (blocked_n > 0) {
+      const int64_t nl = (int64_t)blocked_n * blocked_l;
+      const int i = (int)(c / nl), j = (int)((c - i * nl) / blocked_l);
+      lc = 4 * (int64_t)blk_index(bm, i, j, (int)(c - i * nl - (int64_t)j * blocked_l));
+    }
     // rhs = -2 f h h ; grad_f = -lambda * rhs  (Eikonal3D.cpp:163-166,244-246)
     const double rhs = __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f[c]), h), h);
-    grad_f[c] = __dmul_rn(-lam[c * lam_stride], rhs);
+    grad_f[c] = __dmul_rn(-lam[lc], rhs);
     if (grad_u0) grad_u0[c] = (u[c] == u0[c]) ? gu[c] : 0.0;
   }
 }
@@ -282,21 +290,21 @@ int eik3d_single_adjoint(const double* d_gu, const double* d_u, const double* d_
   SingleWork& W = work(dev);
   std::lock_guard<std::mutex> lock(W.mu);
   const Geom g = make_geom(m, n, l, SBK);
-  if (g.ncell < ((int64_t)1 << 31)) {
+  if (blk_slots(m, n, l) < ((int64_t)1 << 31)) {
     // causal order: every cell evaluated once, after its users, in one CTA
     // (the same per-cell formula as the sweeps below, so the same bits)
     ADT_CUDA(W.scalar.reserve(sizeof(unsigned long long)));
-    ADT_CUDA(W.meta.reserve((size_t)g.ncell * sizeof(uint32_t)));
-    ADT_CUDA(W.rec.reserve((size_t)g.ncell * CAUSAL_REC64_BYTES));
+    const int64_t slots = blk_slots(m, n, l);
+    ADT_CUDA(W.meta.reserve((size_t)slots * sizeof(uint32_t)));
+    ADT_CUDA(W.rec.reserve((size_t)slots * CAUSAL_REC64_BYTES));
     ADT_CUDA(W.queue.reserve((size_t)g.ncell * sizeof(int)));
     int* d_complete = W.scalar.as<int>();
     int rc;
     if ((rc = causal_single_adjoint(d_u, d_u0, d_gu, m, n, l, W.meta.as<uint32_t>(), W.rec.p,
                                     W.queue.as<int>(), d_complete, stream)))
       return rc;
-    k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(W.rec.as<double>(),
-                                                  (int)(CAUSAL_REC64_BYTES / sizeof(double)), d_f,
-                                                  d_u, d_u0, d_gu, h, g.ncell, d_gf, d_gu0);
+    k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(W.rec.as<double>(), n, l, d_f, d_u, d_u0, d_gu, h,
+                                                  g.ncell, d_gf, d_gu0);
     ADT_CUDA(cudaGetLastError());
     int complete = 0;
     ADT_CUDA(cudaMemcpyAsync(&complete, d_complete, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -348,7 +356,7 @@ int eik3d_single_adjoint(const double* d_gu, const double* d_u, const double* d_
       break;
     }
   }
-  k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(lam, 1, d_f, d_u, d_u0, d_gu, h, g.ncell, d_gf, d_gu0);
+  k_grad<<<grid_for(g.ncell), 256, 0, stream>>>(lam, 0, 0, d_f, d_u, d_u0, d_gu, h, g.ncell, d_gf, d_gu0);
   ADT_CUDA(cudaGetLastError());
   ADT_CUDA(cudaStreamSynchronize(stream));
   if (iters_out) *iters_out = done ? it + 1 : it;
