@@ -54,7 +54,7 @@ class BatchStats(C.Structure):
                 ("fwd_bricks", C.c_int64), ("adj_bricks", C.c_int64), ("fwd_ms", C.c_float),
                 ("adj_ms", C.c_float), ("total_ms", C.c_float), ("bk", C.c_int32),
                 ("warps", C.c_int32), ("groups", C.c_int32), ("ctas", C.c_int32),
-                ("adj_warps", C.c_int32), ("adj_groups", C.c_int32)]
+                ("adj_warps", C.c_int32), ("adj_groups", C.c_int32), ("adj_solver", C.c_int32)]
 
 
 _P = C.c_void_p

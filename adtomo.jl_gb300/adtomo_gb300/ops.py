@@ -128,7 +128,8 @@ class Batch3D:
     for the adjoint) leave their neighbours asleep.  adj_solver "causal"
     (ADT_ADJ_CAUSAL) solves each adjoint system once in reverse causal order
     instead of by sweeps ("sweeps", ADT_ADJ_SWEEPS); "auto" (the default)
-    takes the causal solve in FP64 and the sweeps in FP32.
+    starts with the causal solve and, in FP32, lets autotune() keep whichever
+    of the two is faster on the uploaded inputs (stats().adj_solver).
     """
 
     def __init__(self, fields, stations, solve_field, src_xyz, precision=ADT_F32, tol=1e-6,

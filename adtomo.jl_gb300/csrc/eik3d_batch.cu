@@ -184,6 +184,10 @@ struct BatchPlan {
   int fwd_warps = 8, adj_warps = 4, fwd_ctas = 0, adj_ctas = 0;
   int fwd_gw = 4, fwd_groups = 2, adj_gw = 2, adj_groups = 4;
   bool causal = false;  // adjoint in causal order (k_batch_adj_causal, one solve per CTA)
+  bool dual = false;    // both adjoint solvers available (FP32 with ADT_ADJ_AUTO): the
+                        // autotuner keeps the faster
+  const void* adj_kern[2] = {nullptr, nullptr};  // [0] sweeps, [1] causal order
+  int adj_regs_k[2] = {0, 0}, adj_maxt_k[2] = {1024, 1024};
   int max_nb = 0, meta_smem = 0;
   int sm_count = 0, fwd_regs = 0, adj_regs = 0, adj_maxt = 1024;
   size_t smem_budget = 0, fwd_wbytes = 0, adj_wbytes = 0;
@@ -273,7 +277,7 @@ static int apply_shapes(BatchPlan* P, int fwd_gw, int fwd_groups, int adj_gw, in
     return rc;
   if (P->causal) {  // one solve per CTA of adj_gw warps, static shared memory only
     const int max_warps = std::min(P->adj_maxt / 32, 65536 / std::max(1, P->adj_regs * 32));
-    P->adj_gw = std::max(1, std::min(adj_gw > 0 ? adj_gw : 16, max_warps));
+    P->adj_gw = std::max(1, std::min(adj_gw > 0 ? adj_gw : 32, max_warps));
     P->adj_groups = 1;
     P->adj_smem = 0;
   } else if ((rc = fit_shape(P->ks.adj, P->adj_wbytes, P->adj_regs, 1024, P->meta_smem, P->max_nb,
@@ -295,6 +299,19 @@ static int apply_shapes(BatchPlan* P, int fwd_gw, int fwd_groups, int adj_gw, in
     P->graph = nullptr;
   }
   return ADT_OK;
+}
+
+// Make the sweeps (causal = false) or the causal-order solve the adjoint of
+// the next evaluations (both must have been set up at plan creation).
+static void select_solver(BatchPlan* P, bool causal) {
+  P->causal = causal;
+  P->ks.adj = P->adj_kern[causal ? 1 : 0];
+  P->adj_regs = P->adj_regs_k[causal ? 1 : 0];
+  P->adj_maxt = P->adj_maxt_k[causal ? 1 : 0];
+  if (P->graph) {
+    cudaGraphExecDestroy(P->graph);
+    P->graph = nullptr;
+  }
 }
 
 int batch_check_args(int32_t n_fields, const int32_t* dims, const double* hh, const int32_t* nsta,
@@ -353,13 +370,17 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   (void)minl;
   P->bk = o.bk ? o.bk : 32;
   P->nf = n_fields;
-  P->causal = o.adj_solver == ADT_ADJ_CAUSAL ||
-              (o.adj_solver == ADT_ADJ_AUTO && o.precision == ADT_F64);
-  if (P->causal)
-    for (int f = 0; f < n_fields; ++f)
-      if (blk_slots(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2]) >= ((int64_t)1 << 31))
+  // ADT_ADJ_AUTO: the causal-order solve, and in FP32 also the sweeps, for
+  // the autotuner to choose between
+  P->causal = o.adj_solver == ADT_ADJ_CAUSAL || o.adj_solver == ADT_ADJ_AUTO;
+  P->dual = o.adj_solver == ADT_ADJ_AUTO && o.precision == ADT_F32;
+  for (int f = 0; f < n_fields; ++f)
+    if (P->causal && blk_slots(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2]) >= ((int64_t)1 << 31)) {
+      if (o.adj_solver == ADT_ADJ_CAUSAL)
         return set_error(ADT_EINVAL, "batch: the causal-order adjoint needs fewer than 2^31 cells "
                          "per field (field %d)", f);
+      P->causal = P->dual = false;  // automatic choice: the sweeps
+    }
   int64_t sofs = 0;
   for (int f = 0; f < n_fields; ++f) {
     const Geom g = make_geom(dims[3 * f], dims[3 * f + 1], dims[3 * f + 2], P->bk);
@@ -436,7 +457,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       ch.field_uoff[P->solve_field[s]].push_back(cells);
       // 64-byte aligned solves (the FP32 path uses 16-byte accesses), each
       // also holding the causal-order adjoint's blocked slots
-      const int64_t span = P->causal ? std::max(g.ncell, blk_slots(g.m, g.n, g.l)) : g.ncell;
+      const int64_t span = P->causal ? std::max(g.ncell, blk_slots(g.m, g.n, g.l)) : g.ncell;  // causal or dual
       cells += (span + 15) / 16 * 16;
       bricks += (int64_t)META_ARRAYS_MAX * g.nbx * g.nby * g.nbz;
       seeds += 8LL * P->nsta[P->solve_field[s]];
@@ -484,7 +505,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   for (int k = 0; k < P->nsets; ++k) {
     BatchPlan::ChunkBufs& B = P->cb[k];
     R_(B.u, (size_t)max_cells * es);
-    if (!P->causal) {  // the causal-order adjoint keeps lambda in its records
+    if (!P->causal || P->dual) {  // the causal-order adjoint keeps lambda in its records
       R_(B.lam, (size_t)max_cells * es);
       R_(B.code, (size_t)max_cells * 2);
     }
@@ -495,7 +516,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       R_(B.gdense, (size_t)max_cells * es);
       ADT_CUDA(cudaMemset(B.gdense.p, 0, (size_t)max_cells * es));
     }
-    if (P->causal) {
+    if (P->causal || P->dual) {
       R_(B.meta32, (size_t)max_cells * 4);
       R_(B.rec, (size_t)max_cells * 4 * es);
       R_(B.queue, (size_t)max_cells * 4);
@@ -543,7 +564,6 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     R_(P->d_fields, n_fields * sizeof(FieldDev<double>));
     ADT_CUDA(cudaMemcpy(P->d_fields.p, fdv.data(), n_fields * sizeof(FieldDev<double>), cudaMemcpyHostToDevice));
     P->ks = kernels_for<double>(P->bk);
-    if (P->causal) P->ks.adj = P->ks.adj_causal;
   } else {
     std::vector<FieldDev<float>> fdv(n_fields);
     for (int f = 0; f < n_fields; ++f) {
@@ -561,7 +581,6 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
     R_(P->d_fields, n_fields * sizeof(FieldDev<float>));
     ADT_CUDA(cudaMemcpy(P->d_fields.p, fdv.data(), n_fields * sizeof(FieldDev<float>), cudaMemcpyHostToDevice));
     P->ks = kernels_for<float>(P->bk);
-    if (P->causal) P->ks.adj = P->ks.adj_causal;
   }
   ADT_CUDA(cudaMemcpy(P->d_solves.p, P->solves.data(), n_solves * sizeof(SolveDev), cudaMemcpyHostToDevice));
   {
@@ -600,10 +619,15 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   {
     cudaFuncAttributes fa_f, fa_a;
     ADT_CUDA(cudaFuncGetAttributes(&fa_f, P->ks.fwd));
-    ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->ks.adj));
     P->fwd_regs = fa_f.numRegs;
-    P->adj_regs = fa_a.numRegs;
-    P->adj_maxt = fa_a.maxThreadsPerBlock;
+    P->adj_kern[0] = P->ks.adj;
+    P->adj_kern[1] = P->ks.adj_causal;
+    for (int k = 0; k < 2; ++k) {
+      ADT_CUDA(cudaFuncGetAttributes(&fa_a, P->adj_kern[k]));
+      P->adj_regs_k[k] = fa_a.numRegs;
+      P->adj_maxt_k[k] = fa_a.maxThreadsPerBlock;
+    }
+    select_solver(P.get(), P->causal);
   }
   // the causal-order adjoint's width is warps per CTA, not a sweep group's
   const int adj_w0 = o.adj_warps ? o.adj_warps : (P->causal ? 0 : o.warps);
@@ -793,11 +817,14 @@ int batch_upload(BatchPlan* P, const double* slowness, const double* t_obs, cons
   return ADT_OK;
 }
 
-// Pick the sweep kernels' group widths by timing them on the uploaded
-// inputs: every candidate width runs `reps` evaluations and the fastest
-// forward and adjoint kernel times (CUDA events around each kernel) win; the
-// two kernels are tuned one after the other.  Results do not depend on the
-// shape (the bricks of a level are independent), only the time does.
+// Pick the kernels' launch widths by timing them on the uploaded inputs:
+// every candidate width runs `reps` evaluations and the fastest forward and
+// adjoint kernel times (CUDA events around each kernel) win; the two kernels
+// are tuned one after the other.  With both adjoint solvers available (FP32,
+// ADT_ADJ_AUTO), each solver's widths are timed and the faster solver is
+// kept.  Results do not depend on the width (the bricks of a level, and the
+// cells of the causal order, are independent), only the time does; the two
+// solvers reach the same fixed point of the adjoint system.
 int batch_autotune(BatchPlan* P, int reps) {
   if (P->opts.ref_compat)
     return set_error(ADT_EINVAL, "batch: autotune is not available with ref_compat");
@@ -807,8 +834,6 @@ int batch_autotune(BatchPlan* P, int reps) {
   const int fwd_c[] = {3, 4, 5, 6, 8, 10, 12};
   const int adj_sweeps[] = {2, 3, 4, 6, 7, 8, 9};
   const int adj_causal[] = {4, 8, 12, 16, 24, 32};  // warps per CTA
-  const int* adj_c = P->causal ? adj_causal : adj_sweeps;
-  const int n_adj = P->causal ? 6 : 7;
   auto measure = [&](float& fwd_ms, float& adj_ms) -> int {
     fwd_ms = adj_ms = 1e30f;
     for (int r = 0; r < reps; ++r) {
@@ -833,16 +858,27 @@ int batch_autotune(BatchPlan* P, int reps) {
       best_f = gw;
     }
   }
-  for (int t = 0; t < n_adj; ++t) {
-    const int gw = adj_c[t];
-    if ((rc = apply_shapes(P, best_f, 0, gw, 0))) return rc;
-    if (P->adj_gw != gw) continue;
-    if ((rc = measure(ft, at))) return rc;
-    if (at < best_at) {
-      best_at = at;
-      best_a = gw;
+  // the adjoint: each available solver's widths (with both, the faster solver)
+  bool best_causal = P->causal;
+  const bool solvers[2] = {false, true};
+  for (bool causal : solvers) {
+    if (!P->dual && causal != P->causal) continue;
+    select_solver(P, causal);
+    const int* adj_c = causal ? adj_causal : adj_sweeps;
+    const int n_adj = causal ? 6 : 7;
+    for (int t = 0; t < n_adj; ++t) {
+      const int gw = adj_c[t];
+      if ((rc = apply_shapes(P, best_f, 0, gw, 0))) return rc;
+      if (P->adj_gw != gw) continue;
+      if ((rc = measure(ft, at))) return rc;
+      if (at < best_at) {
+        best_at = at;
+        best_a = gw;
+        best_causal = causal;
+      }
     }
   }
+  select_solver(P, best_causal);
   return apply_shapes(P, best_f, 0, best_a, 0);
 }
 
@@ -911,6 +947,7 @@ int batch_stats(BatchPlan* P, adt_batch_stats* s) {
   s->ctas = P->fwd_ctas;
   s->adj_warps = P->adj_gw;
   s->adj_groups = P->adj_groups;
+  s->adj_solver = P->causal ? ADT_ADJ_CAUSAL : ADT_ADJ_SWEEPS;
   s->fwd_ms = s->adj_ms = s->total_ms = -1.f;
   if (!P->ran) return ADT_OK;
   ADT_CUDA(cudaStreamSynchronize(P->stream));

@@ -289,7 +289,8 @@ def run_ours(args, rank, world):
                   adj_solver=args.adj_solver)
     B.upload([f], t_obs, w)
     if args.autotune and not (args.warps or args.groups or args.adj_warps or args.adj_groups):
-        B.autotune(reps=2)  # launch shapes timed on this workload (setup, untimed)
+        B.autotune(reps=2)  # launch shapes (and adjoint solver) timed on this workload, untimed
+    solver_used = "causal" if B.stats().adj_solver == A.ADT_ADJ_CAUSAL else "sweeps"
     stream = torch.cuda.ExternalStream(B.stream())
     for _ in range(args.warmup):
         B.run_resident()
@@ -332,7 +333,8 @@ def run_ours(args, rank, world):
     if rank == 0 and (args.wake_tol > 0 or args.adj_wake_tol > 0):
         # untimed: the same evaluation with exact brick skipping, as the yardstick of
         # what the wake tolerances changed
-        E = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6)
+        E = A.Batch3D([(M, N, L, H)], [sta], sf, src, precision=A.ADT_F32, tol=1e-6,
+                      adj_solver=solver_used)
         _, tp_x, g_x, _ = E.run([f], t_obs, w)
         E.close()
         vs_exact = {"t_pred_max_rel": float(np.max(np.abs(tp - tp_x) / np.abs(tp_x))),
@@ -353,14 +355,15 @@ def run_ours(args, rank, world):
     if os.path.exists(prof) and N_EVENTS == 256:
         try:
             d = json.load(open(prof))
-            traffic = {k: d[k]["traffic_bytes_per_launch"] for k in ("k_batch_fwd", "k_batch_adj")}
+            traffic = {k: d[k]["traffic_bytes_per_launch"] for k in d if k.startswith("k_batch_")}
         except (OSError, ValueError, KeyError):
             traffic = {}
     kern = {
         "k_batch_fwd": {"launch_ms": fwd_ms[-1], "cell_updates": int(upd_f[-1]),
                         "bytes_per_update": BYTES_PER_FWD_UPDATE},
-        "k_batch_adj": {"launch_ms": adj_ms[-1], "cell_updates": int(upd_a[-1]),
-                        "bytes_per_update": BYTES_PER_ADJ_UPDATE},
+        ("k_batch_adj_causal" if solver_used == "causal" else "k_batch_adj"): {
+            "launch_ms": adj_ms[-1], "cell_updates": int(upd_a[-1]),
+            "bytes_per_update": BYTES_PER_ADJ_UPDATE},
     }
     for k, v in kern.items():
         v["achieved_GBs"] = v["cell_updates"] * v["bytes_per_update"] / (v["launch_ms"] / 1e3) / 1e9
@@ -383,7 +386,7 @@ def run_ours(args, rank, world):
         k = cpu_sample
         E = A.Batch3D([(M, N, L, H)], [sta], np.zeros(k, np.int32), src[:k], precision=A.ADT_F32,
                       tol=args.tol, wake_tol=args.wake_tol, adj_wake_tol=args.adj_wake_tol,
-                      fwd_order_filter=bool(args.fwd_order_filter), adj_solver=args.adj_solver)
+                      fwd_order_filter=bool(args.fwd_order_filter), adj_solver=solver_used)
         mis_k, tp_k, (g_k,), _ = E.run([f], t_obs[:k * N_STA], w[:k * N_STA])
         E.close()
         mo, tpo, go = cpu_out
@@ -431,6 +434,7 @@ def run_ours(args, rank, world):
                    "adj_iters_mean": float(np.mean([s.adj_iters for s in status])),
                    "tol": args.tol, "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
                    "fwd_order_filter": args.fwd_order_filter, "adj_solver": args.adj_solver,
+                   "adj_solver_used": solver_used,
                    "picks": "FP64 travel times on the +2%-noise model (reference stopping rule)",
                    "vs_exact_skipping": vs_exact, "error_vs_fp64": err64},
         "e2e": {"value": e2e_val, "unit": "events/s", "h2d_bytes_per_step": h2d,
@@ -453,7 +457,7 @@ def run_ours(args, rank, world):
         "fp64_batched": f64b,
         "clocks": clocks,
         # per evaluation of the one-field, one-chunk plan: k_to_t_f32, k_src_init,
-        # k_batch_fwd, k_batch_misfit, k_batch_adj, k_batch_grad, k_grad_scale,
+        # k_batch_fwd, k_batch_misfit, k_batch_adj or k_batch_adj_causal, k_batch_grad, k_grad_scale,
         # k_misfit_sum, k_order_by_cost
         "gpu_launches": 9 * args.steps,
     }
@@ -531,7 +535,9 @@ def run_large(args):
                    "shapes": {"warps": st.warps, "groups": st.groups, "adj_warps": st.adj_warps,
                               "adj_groups": st.adj_groups},
                    "wake_tol": args.wake_tol, "adj_wake_tol": args.adj_wake_tol,
-                   "adj_solver": args.adj_solver, "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
+                   "adj_solver": args.adj_solver,
+                   "adj_solver_used": "causal" if st.adj_solver == A.ADT_ADJ_CAUSAL else "sweeps",
+                   "fwd_ms": st.fwd_ms, "adj_ms": st.adj_ms,
                    "cell_updates_per_s": (st.fwd_cell_updates + st.adj_cell_updates) /
                    (ms_step / 1000.0),
                    "fwd_iters_mean": float(np.mean([x.iters for x in status])),
@@ -792,8 +798,8 @@ def main():
                     help="adjoint: the same for relative changes (default 1e-4; 0 = exact)")
     ap.add_argument("--adj-solver", default="auto", choices=["auto", "sweeps", "causal"],
                     help="adjoint: reverse sweeps until nothing changes, one evaluation per "
-                         "cell in reverse causal order, or auto (the library default: causal "
-                         "in FP64, sweeps in FP32)")
+                         "cell in reverse causal order, or auto (the library default: causal, "
+                         "and in FP32 the autotuner keeps the faster of the two)")
     ap.add_argument("--fwd-order-filter", type=int, default=1,
                     help="1 (library default): FP32 forward sweeps each brick only in the "
                          "orderings that follow its learned upwind directions; 0: all")

@@ -168,7 +168,7 @@ int adt_eikonal_three_d_device_noalloc(const double* u0, const double* f, double
 /* adjoint solvers of the batched plan (adt_batch_opts.adj_solver) */
 #define ADT_ADJ_SWEEPS 0 /* reverse sweeps until nothing changes (brick skipping, filters) */
 #define ADT_ADJ_CAUSAL 1 /* one evaluation per cell in reverse causal order */
-#define ADT_ADJ_AUTO 2   /* causal in FP64, sweeps in FP32 (each the faster there) */
+#define ADT_ADJ_AUTO 2   /* causal; in FP32 adt_batch_autotune also times the sweeps */
 /* Receivers per field.  Up to 1024 the seed merge runs in shared memory;
  * above, in device scratch of about 128 bytes per receiver per resident solve. */
 #define ADT_BATCH_MAX_RECEIVERS 65536
@@ -209,8 +209,8 @@ typedef struct adt_batch_opts {
                            chunk at a time.  Not with ref_compat. */
   int32_t adj_warps;    /* adjoint kernel's warps per solve: 0 = as `warps` */
   int32_t adj_groups;   /* adjoint kernel's solves per CTA: 0 = as `groups` */
-  int32_t adj_solver;   /* ADT_ADJ_AUTO (default), ADT_ADJ_SWEEPS or ADT_ADJ_CAUSAL:
-                           the adjoint system of a solve is triangular in travel-time order
+  int32_t adj_solver;   /* ADT_ADJ_AUTO (default), ADT_ADJ_SWEEPS or ADT_ADJ_CAUSAL.
+                           The adjoint system of a solve is triangular in travel-time order
                            (a cell's row reads only its users, whose travel times
                            are larger), so it is solved by evaluating every cell
                            once, after its users, in rounds of cells whose users
@@ -218,11 +218,12 @@ typedef struct adt_batch_opts {
                            adj_groups and the adjoint wake tolerance and filter
                            ignored).  Same formula per cell: the exact sweeps'
                            fixed point.  Needs fewer than 2^31 cells per field.
-                           The causal solve gathers each cell's neighbours from
-                           memory, so it is bound by scattered accesses; it wins
-                           where a sweep update is expensive (FP64: 14x on
-                           128x128x64) and loses in FP32, where the sweeps run
-                           from shared-memory tiles. */
+                           Which is faster depends on the model: one causal pass
+                           against the sweeps' iterations, which rough models
+                           need more of.  ADT_ADJ_AUTO starts with the causal
+                           solve; in FP32 it also keeps the sweeps' buffers and
+                           adt_batch_autotune times both and keeps the faster
+                           (adt_batch_stats.adj_solver tells which runs). */
 } adt_batch_opts;
 
 typedef struct adt_batch adt_batch;
@@ -290,6 +291,8 @@ typedef struct adt_batch_stats {
   int32_t ctas;
   int32_t adj_warps;  /* the same for the adjoint kernel */
   int32_t adj_groups;
+  int32_t adj_solver; /* the adjoint solver the evaluations use: ADT_ADJ_SWEEPS or
+                         ADT_ADJ_CAUSAL */
 } adt_batch_stats;
 int adt_batch_stats_get(adt_batch* b, adt_batch_stats* out);
 

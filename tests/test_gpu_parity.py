@@ -444,7 +444,8 @@ def test_batch_fp32_wake_tolerances_against_fp64():
     for kw in ({"wake_tol": 1e-6, "adj_wake_tol": 1e-5}, {"wake_tol": 1e-6, "adj_wake_tol": 1e-5,
                                                           "warps": 3, "groups": 2},
                {"wake_tol": 1e-5, "adj_wake_tol": 1e-4}):
-        B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6, **kw)
+        B = A.Batch3D(fields, stations, sf, src, precision=A.ADT_F32, tol=1e-6,
+                      adj_solver="sweeps", **kw)
         mis, tp, grads, st = B.run(slow, t_obs, w)
         # tolerances: travel times 1e-4 relative, gradient 1e-3 relative (L2)
         assert np.max(np.abs(tp[ok] - tpo[ok]) / tpo[ok]) <= 1e-4, kw
