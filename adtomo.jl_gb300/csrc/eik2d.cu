@@ -18,6 +18,7 @@
 
 #include "eik2d.h"
 #include "eik3d_common_host.h"
+#include "causal_sync.cuh"
 #include "eik_local.cuh"
 
 namespace adt {
@@ -195,6 +196,127 @@ __global__ void k_eik2d_adjoint(const double* __restrict__ gu, const double* __r
   if (threadIdx.x == 0) status[0] = s_singular ? -1 : (done ? it + 1 : 0);
 }
 
+// The 2D adjoint in causal order, one CTA: the rows of k_eik2d_adjoint
+// (Eikonal.h:95-200) solved once, every cell after its users (Kahn's
+// algorithm on the users graph, acyclic since a user's travel time is
+// strictly larger).  A cell's users are the non-source neighbours whose
+// upwind neighbour along the axis is the cell; per cell a word holds their
+// bits (0-3: x-, x+, y-, y+) and, in bits 8-11, those not yet evaluated.
+// Each evaluated non-source cell clears its bit in its upwind neighbours'
+// words (acq_rel atomics at CTA scope); the thread that empties a word queues
+// that cell (release store; slots are read with acquire loads).  The
+// per-cell formula and summation order are k_eik2d_adjoint's, so lambda is
+// the same, bit for bit.  status: 1 done, -1 a non-source cell has no upwind
+// direction, 0 a wait on the queue ran out (bounded by CAUSAL_WAIT_CYCLES).
+__global__ void __launch_bounds__(512)
+    k_eik2d_adjoint_causal(const double* __restrict__ gu, const double* __restrict__ u,
+                           const double* __restrict__ f, int m, int n, double h, int ix, int jx,
+                           double* lam, double* __restrict__ grad_f, uint32_t* word, int* queue,
+                           int* __restrict__ status) {
+  __shared__ int s_head, s_tail, s_err, s_singular;
+  const int w = m + 1;
+  const int N = (m + 1) * (n + 1);
+  const int src = jx * w + ix;
+  const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_head = s_tail = 0;
+    s_err = s_singular = 0;
+  }
+  for (int p = tid; p < N; p += nth) queue[p] = -1;
+  __syncthreads();
+  // users of each cell, cells without users queued, singular rows found
+  for (int c0 = warp * 32; c0 < N; c0 += nth) {
+    const int c = c0 + lane;
+    uint32_t us = 0;
+    if (c < N) {
+      const int i = c % w, j = c / w;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int ri = i + (q == 0 ? -1 : q == 1 ? 1 : 0);
+        const int rj = j + (q == 2 ? -1 : q == 3 ? 1 : 0);
+        if (ri < 0 || ri > m || rj < 0 || rj > n) continue;
+        const int r = rj * w + ri;
+        if (r == src) continue;
+        const int64_t nb = (q < 2) ? upw2(u, r, ri, m, 1) : upw2(u, r, rj, n, w);
+        if (nb == c && u[r] > u[c]) us |= 1u << q;
+      }
+      word[c] = us | (us << 8);
+      if (c != src && !(u[c] > u[upw2(u, c, i, m, 1)]) && !(u[c] > u[upw2(u, c, j, n, w)]))
+        s_singular = 1;
+    }
+    const int pos = warp_append((c < N && us == 0) ? 1 : 0, &s_tail, lane);
+    if (c < N && us == 0) queue[pos] = c;
+  }
+  __syncthreads();
+  if (!s_singular) {
+    for (;;) {
+      const int slot = take_slots(1, &s_head);
+      if (slot >= N) break;
+      int x = ld_acquire_cta(queue + slot);
+      if (x < 0) {
+        const long long t0 = clock64();
+        do {
+          __nanosleep(64);
+          x = ld_acquire_cta(queue + slot);
+        } while (x < 0 && clock64() - t0 < CAUSAL_WAIT_CYCLES &&
+                 !*reinterpret_cast<volatile int*>(&s_err));
+        if (x < 0) {  // out of budget, or another thread's was
+          atomicOr(&s_err, 1);
+          break;
+        }
+      }
+      const int i = x % w, j = x / w;
+      const uint32_t us = word[x] & 15u;
+      double acc = gu[x];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if ((us >> q) & 1u) {
+          const int r = x + (q == 0 ? -1 : q == 1 ? 1 : q == 2 ? -w : w);
+          acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(2.0, __dsub_rn(u[r], u[x])), lam[r]));
+        }
+      double d;
+      const int nx = (int)upw2(u, x, i, m, 1), ny = (int)upw2(u, x, j, n, w);
+      if (x == src) {
+        d = 1.0;
+      } else {
+        d = 0.0;
+        if (u[x] > u[nx]) d = __dadd_rn(d, __dmul_rn(2.0, __dsub_rn(u[x], u[nx])));
+        if (u[x] > u[ny]) d = __dadd_rn(d, __dmul_rn(2.0, __dsub_rn(u[x], u[ny])));
+      }
+      lam[x] = __ddiv_rn(acc, d);
+      // release the upwind neighbours this cell is a user of
+      int rel[2] = {-1, -1}, np = 0;
+      if (x != src) {
+        const int nbs[2] = {nx, ny};
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          const int nb = nbs[a];
+          if (!(u[x] > u[nb])) continue;
+          // this cell seen from nb: x+ (1) or x- (0), y+ (3) or y- (2)
+          const int q = a == 0 ? (nb < x ? 1 : 0) : (nb < x ? 3 : 2);
+          const uint32_t bit = (1u << q) << 8;
+          const uint32_t old = atom_and_acq_rel_cta(word + nb, ~bit);
+          if ((old & bit) && !(old & ~bit & 0xf00u)) {
+            rel[a] = nb;
+            ++np;
+          }
+        }
+      }
+      int pos = take_slots(np, &s_tail);
+      for (int a = 0; a < 2; ++a)
+        if (rel[a] >= 0) st_release_cta(queue + pos++, rel[a]);
+    }
+  }
+  __syncthreads();
+  const bool done = !s_singular && !s_err && s_tail == N;
+  for (int p = tid; p < N; p += nth) {
+    // dFdf = -2 f h h, 0 at the source; grad_f = -lambda * dFdf (Eikonal.h:100-104,196-198)
+    const double dfdf = (p == src) ? 0.0 : __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f[p]), h), h);
+    grad_f[p] = done ? __dmul_rn(-lam[p], dfdf) : 0.0;
+  }
+  if (tid == 0) status[0] = s_singular ? -1 : (done ? 1 : 0);
+}
+
 int eik2d_forward_batch(const double* d_f, int m, int n, double h, int count, const int* d_srcx,
                         const int* d_srcy, double* d_u, adt_solve_status* st, cudaStream_t stream) {
   const int64_t N = (int64_t)(m + 1) * (n + 1);
@@ -232,14 +354,23 @@ int eik2d_adjoint(const double* d_gu, const double* d_u, const double* d_f, int 
   DevBuf lam, stat;
   ADT_CUDA(lam.reserve((size_t)N * sizeof(double)));
   ADT_CUDA(stat.reserve(sizeof(int)));
-  k_eik2d_adjoint<<<1, 256, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, lam.as<double>(), d_gf,
-                                         stat.as<int>());
+  if (N < (1 << 30)) {  // causal order: every cell once
+    DevBuf word, queue;
+    ADT_CUDA(word.reserve((size_t)N * sizeof(uint32_t)));
+    ADT_CUDA(queue.reserve((size_t)N * sizeof(int)));
+    k_eik2d_adjoint_causal<<<1, 512, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, lam.as<double>(),
+                                                  d_gf, word.as<uint32_t>(), queue.as<int>(),
+                                                  stat.as<int>());
+  } else {
+    k_eik2d_adjoint<<<1, 256, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, lam.as<double>(), d_gf,
+                                           stat.as<int>());
+  }
   ADT_CUDA(cudaGetLastError());
   int s = 0;
   ADT_CUDA(cudaMemcpyAsync(&s, stat.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
   ADT_CUDA(cudaStreamSynchronize(stream));
   if (s < 0) return set_error(ADT_ESINGULAR, "2D adjoint: a non-source cell has no upwind direction");
-  if (s == 0) return set_error(ADT_ENOCONV, "2D adjoint sweeps did not settle");
+  if (s == 0) return set_error(ADT_ENOCONV, "2D adjoint did not complete");
   return ADT_OK;
 }
 

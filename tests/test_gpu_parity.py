@@ -169,6 +169,23 @@ def test_2d_c1_config_forward_and_grad():
     assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 1.0))
 
 
+def test_2d_adjoint_singular_row_is_an_error():
+    """A non-source cell with no upwind direction (u smaller than all four
+    neighbours away from the source) leaves its adjoint row without a
+    diagonal: ADT_ESINGULAR, where the reference's SparseLU fails silently.
+    The same travel times without that minimum give a finite gradient."""
+    m = n = 12
+    f = np.ones((n + 1, m + 1))
+    u = A.eikonal(f, 4, 4, 1.0)
+    gu = np.ones_like(u)
+    assert np.all(np.isfinite(A.eikonal_grad(gu, u, f, 4, 4, 1.0)))
+    bad = u.copy()
+    bad[9, 9] = min(bad[8, 9], bad[10, 9], bad[9, 8], bad[9, 10]) - 0.5
+    with pytest.raises(A.AdtError) as e:
+        A.eikonal_grad(gu, bad, f, 4, 4, 1.0)
+    assert e.value.name == "ADT_ESINGULAR"
+
+
 def test_2d_batch_matches_single_solves():
     rng = np.random.default_rng(4)
     f = rng.uniform(0.5, 1.5, size=(23, 31))
