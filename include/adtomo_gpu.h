@@ -255,10 +255,13 @@ int adt_batch_run(adt_batch* b, const double* slowness, const double* t_obs, con
 int adt_batch_set_source_velocity(adt_batch* b, const double* vel0);
 
 /* Autotuner of the launch shapes: after adt_batch_upload of all three
- * inputs, times the forward and the adjoint sweep kernels over candidate
- * warp-group widths (reps evaluations each, 1-16) on those inputs and keeps
- * the fastest of each (visible in adt_batch_stats_get).  Results do not
- * depend on the shape.  Not available with ref_compat. */
+ * inputs, times the forward and the adjoint kernels over candidate widths
+ * (reps evaluations each, 1-16) on those inputs and keeps the fastest of each
+ * (visible in adt_batch_stats_get).  With both adjoint solvers available
+ * (ADT_ADJ_AUTO in FP32) it times both and keeps the faster solver.  Results
+ * do not depend on the width; the two solvers reach the same fixed point of
+ * the adjoint system (bit for bit on depths that are multiples of 8).  Not
+ * available with ref_compat. */
 int adt_batch_autotune(adt_batch* b, int32_t reps);
 
 /* Device-resident use: upload inputs once, run, read outputs later.  upload
