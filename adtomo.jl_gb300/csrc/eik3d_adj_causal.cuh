@@ -1,5 +1,6 @@
-// eik3d_adj_causal.cuh -- the batched plan's adjoint solved once, in causal
-// order, instead of by sweeps until nothing changes.
+// eik3d_adj_causal.cuh -- the 3D adjoint solved once, in causal order,
+// instead of by sweeps until nothing changes: the batched plan's
+// (k_batch_adj_causal) and the single-event op's (k_single_adj_causal).
 //
 // The adjoint system of one solve (Eikonal3D.cpp:96-198, which assembles it
 // and factors it with SparseLU) is triangular in travel-time order: cell c's
@@ -48,8 +49,8 @@
 #include "causal_sync.cuh"
 #include "eik3d_batch_kernels.cuh"
 
-// Threads per CTA the kernel is compiled for: FP32 1024 (64 registers), FP64
-// 512 (its doubles need more registers).
+// Threads per CTA the kernels are compiled for: FP32 1024 (at most 64
+// registers; the kernel needs about 42), FP64 512 (its doubles need more).
 #ifndef ADT_CAUSAL_MAXT
 #define ADT_CAUSAL_MAXT 1024
 #endif
