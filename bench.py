@@ -461,8 +461,36 @@ def run_ours(args, rank, world):
         # k_misfit_sum, k_order_by_cost
         "gpu_launches": 9 * args.steps,
     }
-    print(json.dumps(line), flush=True)
     B.close()
+    if args.secondary:
+        line["secondary"] = secondary_results(args)
+    print(json.dumps(line), flush=True)
+
+
+def secondary_results(args):
+    """The other configurations, measured after the headline (outside its
+    timed region) so that one default run covers them: C1 and C2 (the plain
+    FP64 ops, one event, host buffers, against the oracle port on one core,
+    with parity) and C4 (the uneven P/S batch, adjoint solver chosen by the
+    autotuner).  C5 and the inversions take minutes: --workload c5 / c5inv /
+    inversion."""
+    import copy
+    out = {}
+    for wl, steps, warmup in (("c1", 10, 2), ("c2", 3, 1)):
+        a = copy.copy(args)
+        a.workload, a.steps, a.warmup = wl, steps, warmup
+        r = run_single(a, emit=False)
+        out[wl] = {"workload": r["config"]["workload"], "gpu_ms_per_event": r["value"],
+                   "cpu_ms_per_event": r["cpu_baseline"]["value"], "parity": r["parity"]}
+    a = copy.copy(args)
+    a.workload, a.steps, a.warmup = "c4", 3, 1
+    r = run_large(a, emit=False)
+    c = r["config"]
+    out["c4"] = {"workload": c["workload"], "solves_per_s": r["value"],
+                 "ms_per_evaluation": r["ms_per_step"], "fwd_ms": c["fwd_ms"], "adj_ms": c["adj_ms"],
+                 "adj_solver_used": c["adj_solver_used"], "shapes": c["shapes"],
+                 "all_converged": c["all_converged"]}
+    return out
 
 
 def large_workload(name, rng):
@@ -494,8 +522,9 @@ def large_workload(name, rng):
     return [(m, n, l, 0.25)], [sta], [f], np.zeros(2000, np.int32), src, 128, desc
 
 
-def run_large(args):
-    """Secondary lines for the larger configurations (not the headline)."""
+def run_large(args, emit=True):
+    """Secondary lines for the larger configurations (not the headline);
+    returns the line (printed when emit)."""
     import torch
     import adtomo_gb300 as A
     rng = np.random.default_rng(SEED)
@@ -544,11 +573,13 @@ def run_large(args):
                    "adj_iters_mean": float(np.mean([x.adj_iters for x in status])),
                    "all_converged": bool(all(x.converged and x.adj_converged for x in status))},
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
     B.close()
+    return line
 
 
-def run_single(args):
+def run_single(args, emit=True):
     """Secondary lines for the plain FP64 configurations (one event, no
     batching), GPU through the host-pointer API against the oracle port of the
     reference's CPU op on one core, with parity:
@@ -629,7 +660,9 @@ def run_single(args):
         "parity": {"forward_bit_identical": bool(np.array_equal(u, ur)),
                    "grad_max_rel": float(np.max(np.abs(gf - rf)) / np.max(np.abs(rf)))},
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_inversion(args):
@@ -815,6 +848,8 @@ def main():
                     help="c5inv: events of the FP32-vs-FP64 comparison (0 skips it)")
     ap.add_argument("--c5-fp64-iters", type=int, default=2,
                     help="c5inv: L-BFGS iterations of the FP32-vs-FP64 comparison")
+    ap.add_argument("--secondary", type=int, default=1,
+                    help="c3: also measure C1, C2 and C4 after the headline (0 skips)")
     ap.add_argument("--fp64-batched", type=int, default=1,
                     help="1: time the same batched plan in FP64 as a yardstick (untimed leg)")
     args = ap.parse_args()
