@@ -471,9 +471,10 @@ def secondary_results(args):
     """The other configurations, measured after the headline (outside its
     timed region) so that one default run covers them: C1 and C2 (the plain
     FP64 ops, one event, host buffers, against the oracle port on one core,
-    with parity) and C4 (the uneven P/S batch, adjoint solver chosen by the
-    autotuner).  C5 and the inversions take minutes: --workload c5 / c5inv /
-    inversion."""
+    with parity), C4 (the uneven P/S batch, adjoint solver chosen by the
+    autotuner) and one C5 evaluation (2000 events in 128-event chunks, the
+    shapes the autotuner picks there).  The inversions take minutes:
+    --workload c5inv / inversion."""
     import copy
     out = {}
     for wl, steps, warmup in (("c1", 10, 2), ("c2", 3, 1)):
@@ -482,14 +483,19 @@ def secondary_results(args):
         r = run_single(a, emit=False)
         out[wl] = {"workload": r["config"]["workload"], "gpu_ms_per_event": r["value"],
                    "cpu_ms_per_event": r["cpu_baseline"]["value"], "parity": r["parity"]}
-    a = copy.copy(args)
-    a.workload, a.steps, a.warmup = "c4", 3, 1
-    r = run_large(a, emit=False)
-    c = r["config"]
-    out["c4"] = {"workload": c["workload"], "solves_per_s": r["value"],
-                 "ms_per_evaluation": r["ms_per_step"], "fwd_ms": c["fwd_ms"], "adj_ms": c["adj_ms"],
-                 "adj_solver_used": c["adj_solver_used"], "shapes": c["shapes"],
-                 "all_converged": c["all_converged"]}
+    for wl, steps, shapes in (("c4", 3, None), ("c5", 1, (12, 1, 32))):
+        a = copy.copy(args)
+        a.workload, a.steps, a.warmup = wl, steps, 1
+        if shapes:  # C5: the shapes the autotuner picks there (forward 12 x 1, causal 32)
+            a.autotune = 0
+            a.warps, a.groups, a.adj_warps, a.adj_groups = shapes[0], shapes[1], shapes[2], 0
+        r = run_large(a, emit=False)
+        c = r["config"]
+        out[wl] = {"workload": c["workload"], "solves_per_s": r["value"],
+                   "ms_per_evaluation": r["ms_per_step"], "fwd_ms": c["fwd_ms"],
+                   "adj_ms": c["adj_ms"], "adj_solver_used": c["adj_solver_used"],
+                   "shapes": c["shapes"], "autotuned": bool(a.autotune),
+                   "all_converged": c["all_converged"]}
     return out
 
 
@@ -849,7 +855,7 @@ def main():
     ap.add_argument("--c5-fp64-iters", type=int, default=2,
                     help="c5inv: L-BFGS iterations of the FP32-vs-FP64 comparison")
     ap.add_argument("--secondary", type=int, default=1,
-                    help="c3: also measure C1, C2 and C4 after the headline (0 skips)")
+                    help="c3: also measure C1, C2, C4 and C5 after the headline (0 skips)")
     ap.add_argument("--fp64-batched", type=int, default=1,
                     help="1: time the same batched plan in FP64 as a yardstick (untimed leg)")
     args = ap.parse_args()
