@@ -14,12 +14,15 @@
 // diagonal sweeps until a full iteration changes nothing.  A non-source cell
 // without an active axis makes the reference's matrix singular; it is
 // reported as ADT_ESINGULAR.
+#include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "eik2d.h"
 #include "eik3d_common_host.h"
 #include "causal_sync.cuh"
 #include "eik_local.cuh"
+#include "fp64_int.cuh"
 
 namespace adt {
 
@@ -44,18 +47,52 @@ __device__ __forceinline__ void ord2(int o, int& si, int& sj) {
   sj = (o >= 2) ? -1 : 1;
 }
 
+// Travel times and change flags of a solve stay in shared memory up to this
+// many nodes (9 bytes each).
+constexpr int FWD2_SMEM_NODES = 25600;
+// The causal adjoint's lambda, queue and flags stay in shared memory up to
+// this many nodes (13 bytes each).
+constexpr int ADJ2_SMEM_NODES = 17600;
+
 }  // namespace
 
-__global__ void k_eik2d_forward(const double* __restrict__ f, int m, int n, double h,
-                                const int* __restrict__ srcx, const int* __restrict__ srcy,
-                                double* __restrict__ u_all, double* __restrict__ prev_all,
-                                int* __restrict__ iters, int* __restrict__ conv,
-                                double* __restrict__ errs) {
+// Per-node constants of the 2D update, formed once per call in the
+// reference's operation order (Eikonal.h:14-20): x = f h, y = 2 f f h h.
+__global__ void k_eik2d_cells(const double* __restrict__ f, int64_t N, double h,
+                              double2* __restrict__ cst) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const double fv = f[p];
+    cst[p] = make_double2(__dmul_rn(fv, h),
+                          __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, fv), fv), h), h));
+  }
+}
+
+// Exact work skipping: a node's update reads only its four neighbours, so a
+// node none of whose neighbours changed since its last update would compute
+// the same candidate again, which cannot lower it.  dirty[c] says a
+// neighbour of c changed since c was last updated (all set at the start);
+// an update clears the node's flag, and a node that decreases sets its
+// neighbours' flags.  Neighbours lie on the adjacent anti-diagonals, so
+// within a wavefront step no flag is set and cleared at once, and the
+// travel times are bit for bit those of updating every node.
+//
+// SMEM: the solve's travel times and flags live in dynamic shared memory
+// (grids up to FWD2_SMEM_NODES nodes), written to u_all at the end;
+// otherwise u_all and dirty_all (N bytes per solve) hold them.
+template <bool SMEM>
+__global__ void __launch_bounds__(512)
+    k_eik2d_forward(const double2* __restrict__ cst, int m, int n, const int* __restrict__ srcx,
+                    const int* __restrict__ srcy, double* __restrict__ u_all,
+                    double* __restrict__ prev_all, uint8_t* __restrict__ dirty_all,
+                    int* __restrict__ iters, int* __restrict__ conv, double* __restrict__ errs) {
+  extern __shared__ double s_u[];
   __shared__ double red[33];
   const int w = m + 1;
   const int64_t N = (int64_t)(m + 1) * (n + 1);
   const int sol = blockIdx.x;
-  double* u = u_all + sol * N;
+  double* u = SMEM ? s_u : u_all + sol * N;
+  uint8_t* dirty = SMEM ? reinterpret_cast<uint8_t*>(s_u + N) : dirty_all + sol * N;
   double* prev = prev_all + sol * N;
   const int ix = srcx[sol], jx = srcy[sol];
   for (int64_t p = threadIdx.x; p < N; p += blockDim.x) {
@@ -63,6 +100,7 @@ __global__ void k_eik2d_forward(const double* __restrict__ f, int m, int n, doub
     const double v = (i == ix && j == jx) ? 0.0 : 100000.0;
     u[p] = v;
     prev[p] = v;
+    dirty[p] = 1;
   }
   __syncthreads();
   int it, done = 0;
@@ -78,15 +116,25 @@ __global__ void k_eik2d_forward(const double* __restrict__ f, int m, int n, doub
           const int i = si > 0 ? a : m - a;
           const int j = sj > 0 ? b : n - b;
           if (i == ix && j == jx) continue;
+          const int c = j * w + i;
+          if (!dirty[c]) continue;
+          dirty[c] = 0;
+          const double2 k = cst[c];
           double ax, by;
-          if (i == 0) ax = u[j * w + 1];
-          else if (i == m) ax = u[j * w + m - 1];
-          else ax = rmin(u[j * w + i + 1], u[j * w + i - 1]);
-          if (j == 0) by = u[w + i];
-          else if (j == n) by = u[(n - 1) * w + i];
-          else by = rmin(u[(j - 1) * w + i], u[(j + 1) * w + i]);
-          const double un = upd2_exact(ax, by, f[j * w + i], h);
-          u[j * w + i] = rmin(u[j * w + i], un);
+          if (i == 0) ax = u[c + 1];
+          else if (i == m) ax = u[c - 1];
+          else ax = rmin(u[c + 1], u[c - 1]);
+          if (j == 0) by = u[c + w];
+          else if (j == n) by = u[c - w];
+          else by = rmin(u[c - w], u[c + w]);
+          const double un = upd2_exact(ax, by, k.x, k.y);
+          if (un < u[c]) {  // rmin(u[c], un)
+            u[c] = un;
+            if (i > 0) dirty[c - 1] = 1;
+            if (i < m) dirty[c + 1] = 1;
+            if (j > 0) dirty[c - w] = 1;
+            if (j < n) dirty[c + w] = 1;
+          }
         }
         __syncthreads();
       }
@@ -107,6 +155,8 @@ __global__ void k_eik2d_forward(const double* __restrict__ f, int m, int n, doub
     for (int64_t p = threadIdx.x; p < N; p += blockDim.x) prev[p] = u[p];
     __syncthreads();
   }
+  if (SMEM)
+    for (int64_t p = threadIdx.x; p < N; p += blockDim.x) u_all[sol * N + p] = u[p];
   if (threadIdx.x == 0) {
     iters[sol] = done ? it + 1 : it;
     conv[sol] = done;
@@ -171,7 +221,7 @@ __global__ void k_eik2d_adjoint(const double* __restrict__ gu, const double* __r
             s_singular = 1;
             continue;
           }
-          const double l = __ddiv_rn(acc, d);
+          const double l = fi_div(acc, d);
           if (!(l == lam[c])) {
             lam[c] = l;
             s_changed = 1;
@@ -200,24 +250,56 @@ __global__ void k_eik2d_adjoint(const double* __restrict__ gu, const double* __r
 // (Eikonal.h:95-200) solved once, every cell after its users (Kahn's
 // algorithm on the users graph, acyclic since a user's travel time is
 // strictly larger).  A cell's users are the non-source neighbours whose
-// upwind neighbour along the axis is the cell; per cell a word holds their
-// bits (0-3: x-, x+, y-, y+) and, in bits 8-11, those not yet evaluated.
-// Each evaluated non-source cell clears its bit in its upwind neighbours'
-// words (acq_rel atomics at CTA scope); the thread that empties a word queues
-// that cell (release store; slots are read with acquire loads).  The
-// per-cell formula and summation order are k_eik2d_adjoint's, so lambda is
-// the same, bit for bit.  status: 1 done, -1 a non-source cell has no upwind
-// direction, 0 a wait on the queue ran out (bounded by CAUSAL_WAIT_CYCLES).
+// upwind neighbour along the axis is the cell; per cell a flag set holds
+// their bits (x-, x+, y-, y+) and those not yet evaluated.  Each evaluated
+// non-source cell clears its bit in its upwind neighbours' sets (acq_rel
+// atomics at CTA scope); the thread that empties a set queues that cell
+// (release store; slots are read with acquire loads).  The per-cell formula
+// and summation order are k_eik2d_adjoint's, so lambda is the same, bit for
+// bit.  status: 1 done, -1 a non-source cell has no upwind direction, 0 a
+// wait on the queue ran out (bounded by CAUSAL_WAIT_CYCLES).
+//
+// SMEM (grids up to ADJ2_SMEM_NODES nodes): lambda, the queue and the flag
+// sets (one byte per cell: users in bits 0-3, outstanding in 4-7, four
+// cells to a 32-bit word for the atomics) live in dynamic shared memory, so
+// the dependent steps of the evaluation chain (queue slot, users' lambda,
+// release) stay on the SM.  Otherwise lam, word (one 32-bit set per cell:
+// users in bits 0-3, outstanding in 8-11) and queue are global.
+template <bool SMEM>
 __global__ void __launch_bounds__(512)
     k_eik2d_adjoint_causal(const double* __restrict__ gu, const double* __restrict__ u,
                            const double* __restrict__ f, int m, int n, double h, int ix, int jx,
-                           double* lam, double* __restrict__ grad_f, uint32_t* word, int* queue,
-                           int* __restrict__ status) {
+                           double* lam_g, double* __restrict__ grad_f, uint32_t* word_g,
+                           int* queue_g, int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char adj_smem[];
   __shared__ int s_head, s_tail, s_err, s_singular;
   const int w = m + 1;
   const int N = (m + 1) * (n + 1);
   const int src = jx * w + ix;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  double* lam = SMEM ? reinterpret_cast<double*>(adj_smem) : lam_g;
+  int* queue = SMEM ? reinterpret_cast<int*>(adj_smem + (size_t)N * 8) : queue_g;
+  uint32_t* word = SMEM ? reinterpret_cast<uint32_t*>(adj_smem + (size_t)N * 12) : word_g;
+  uint8_t* flag = reinterpret_cast<uint8_t*>(word);
+  auto q_load = [&](int slot) {
+    return SMEM ? ld_acquire_cta_shared(queue + slot) : ld_acquire_cta(queue + slot);
+  };
+  auto q_store = [&](int slot, int v) {
+    if (SMEM) st_release_cta_shared(queue + slot, v);
+    else st_release_cta(queue + slot, v);
+  };
+  // clears user bit q of cell nb; true when that emptied its outstanding set
+  auto release = [&](int nb, int q) -> bool {
+    if (SMEM) {
+      const int sh = 8 * (nb & 3);
+      const uint32_t bit = (1u << (q + 4)) << sh;
+      const uint32_t old = atom_and_acq_rel_cta_shared(word + (nb >> 2), ~bit);
+      return (old & bit) && !(old & ~bit & (0xf0u << sh));
+    }
+    const uint32_t bit = (1u << q) << 8;
+    const uint32_t old = atom_and_acq_rel_cta(word + nb, ~bit);
+    return (old & bit) && !(old & ~bit & 0xf00u);
+  };
   if (tid == 0) {
     s_head = s_tail = 0;
     s_err = s_singular = 0;
@@ -240,7 +322,8 @@ __global__ void __launch_bounds__(512)
         const int64_t nb = (q < 2) ? upw2(u, r, ri, m, 1) : upw2(u, r, rj, n, w);
         if (nb == c && u[r] > u[c]) us |= 1u << q;
       }
-      word[c] = us | (us << 8);
+      if (SMEM) flag[c] = (uint8_t)(us | (us << 4));
+      else word[c] = us | (us << 8);
       if (c != src && !(u[c] > u[upw2(u, c, i, m, 1)]) && !(u[c] > u[upw2(u, c, j, n, w)]))
         s_singular = 1;
     }
@@ -252,12 +335,12 @@ __global__ void __launch_bounds__(512)
     for (;;) {
       const int slot = take_slots(1, &s_head);
       if (slot >= N) break;
-      int x = ld_acquire_cta(queue + slot);
+      int x = q_load(slot);
       if (x < 0) {
         const long long t0 = clock64();
         do {
           __nanosleep(64);
-          x = ld_acquire_cta(queue + slot);
+          x = q_load(slot);
         } while (x < 0 && clock64() - t0 < CAUSAL_WAIT_CYCLES &&
                  !*reinterpret_cast<volatile int*>(&s_err));
         if (x < 0) {  // out of budget, or another thread's was
@@ -266,7 +349,7 @@ __global__ void __launch_bounds__(512)
         }
       }
       const int i = x % w, j = x / w;
-      const uint32_t us = word[x] & 15u;
+      const uint32_t us = (SMEM ? (uint32_t)flag[x] : word[x]) & 15u;
       double acc = gu[x];
 #pragma unroll
       for (int q = 0; q < 4; ++q)
@@ -279,11 +362,14 @@ __global__ void __launch_bounds__(512)
       if (x == src) {
         d = 1.0;
       } else {
-        d = 0.0;
-        if (u[x] > u[nx]) d = __dadd_rn(d, __dmul_rn(2.0, __dsub_rn(u[x], u[nx])));
-        if (u[x] > u[ny]) d = __dadd_rn(d, __dmul_rn(2.0, __dsub_rn(u[x], u[ny])));
+        // 0 + t is t for the positive t of an upwind axis: the first term
+        // needs no addition
+        const bool ax = u[x] > u[nx], ay = u[x] > u[ny];
+        const double tx = ax ? __dmul_rn(2.0, __dsub_rn(u[x], u[nx])) : 0.0;
+        const double ty = ay ? __dmul_rn(2.0, __dsub_rn(u[x], u[ny])) : 0.0;
+        d = (ax && ay) ? __dadd_rn(tx, ty) : (ax ? tx : ty);
       }
-      lam[x] = __ddiv_rn(acc, d);
+      lam[x] = fi_div(acc, d);
       // release the upwind neighbours this cell is a user of
       int rel[2] = {-1, -1}, np = 0;
       if (x != src) {
@@ -294,9 +380,7 @@ __global__ void __launch_bounds__(512)
           if (!(u[x] > u[nb])) continue;
           // this cell seen from nb: x+ (1) or x- (0), y+ (3) or y- (2)
           const int q = a == 0 ? (nb < x ? 1 : 0) : (nb < x ? 3 : 2);
-          const uint32_t bit = (1u << q) << 8;
-          const uint32_t old = atom_and_acq_rel_cta(word + nb, ~bit);
-          if ((old & bit) && !(old & ~bit & 0xf00u)) {
+          if (release(nb, q)) {
             rel[a] = nb;
             ++np;
           }
@@ -304,7 +388,7 @@ __global__ void __launch_bounds__(512)
       }
       int pos = take_slots(np, &s_tail);
       for (int a = 0; a < 2; ++a)
-        if (rel[a] >= 0) st_release_cta(queue + pos++, rel[a]);
+        if (rel[a] >= 0) q_store(pos++, rel[a]);
     }
   }
   __syncthreads();
@@ -317,26 +401,57 @@ __global__ void __launch_bounds__(512)
   if (tid == 0) status[0] = s_singular ? -1 : (done ? 1 : 0);
 }
 
+namespace {
+// Device workspaces of the 2D solves, kept per device between calls (grown,
+// never shrunk); a call holds its device's lock while it uses them.
+struct Eik2dWork {
+  std::mutex mu;
+  DevBuf prev, dirty, cst, stat, lam, word, queue;
+};
+Eik2dWork& work2d(int dev) {
+  static Eik2dWork* w = new Eik2dWork[64];
+  return w[dev & 63];
+}
+}  // namespace
+
 int eik2d_forward_batch(const double* d_f, int m, int n, double h, int count, const int* d_srcx,
                         const int* d_srcy, double* d_u, adt_solve_status* st, cudaStream_t stream) {
   const int64_t N = (int64_t)(m + 1) * (n + 1);
-  DevBuf prev, b_it, b_cv, b_err;
-  ADT_CUDA(prev.reserve((size_t)count * N * sizeof(double)));
-  ADT_CUDA(b_it.reserve((size_t)count * sizeof(int)));
-  ADT_CUDA(b_cv.reserve((size_t)count * sizeof(int)));
-  ADT_CUDA(b_err.reserve((size_t)count * sizeof(double)));
-  int* d_iters = b_it.as<int>();
-  int* d_conv = b_cv.as<int>();
-  double* d_err = b_err.as<double>();
-  k_eik2d_forward<<<count, 256, 0, stream>>>(d_f, m, n, h, d_srcx, d_srcy, d_u, prev.as<double>(),
-                                             d_iters, d_conv, d_err);
+  int dev = 0;
+  ADT_CUDA(cudaGetDevice(&dev));
+  Eik2dWork& W = work2d(dev);
+  std::lock_guard<std::mutex> lock(W.mu);
+  ADT_CUDA(W.prev.reserve((size_t)count * N * sizeof(double)));
+  ADT_CUDA(W.cst.reserve((size_t)N * sizeof(double2)));
+  ADT_CUDA(W.stat.reserve((size_t)count * (2 * sizeof(int) + sizeof(double))));
+  double* d_err = W.stat.as<double>();
+  int* d_iters = reinterpret_cast<int*>(d_err + count);
+  int* d_conv = d_iters + count;
+  double2* cst = W.cst.as<double2>();
+  k_eik2d_cells<<<(int)std::min<int64_t>((N + 255) / 256, 1024), 256, 0, stream>>>(d_f, N, h, cst);
   ADT_CUDA(cudaGetLastError());
-  std::vector<int> it(count), cv(count);
-  std::vector<double> er(count);
-  ADT_CUDA(cudaMemcpyAsync(it.data(), d_iters, count * sizeof(int), cudaMemcpyDeviceToHost, stream));
-  ADT_CUDA(cudaMemcpyAsync(cv.data(), d_conv, count * sizeof(int), cudaMemcpyDeviceToHost, stream));
-  ADT_CUDA(cudaMemcpyAsync(er.data(), d_err, count * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  // a wavefront holds at most min(m, n) + 1 nodes
+  const int thr = std::max(64, std::min(512, (std::min(m, n) + 32) / 32 * 32));
+  if (N <= FWD2_SMEM_NODES) {
+    const int smem = (int)(N * (sizeof(double) + 1));
+    ADT_CUDA(cudaFuncSetAttribute(k_eik2d_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem));
+    k_eik2d_forward<true><<<count, thr, smem, stream>>>(cst, m, n, d_srcx, d_srcy, d_u,
+                                                        W.prev.as<double>(), nullptr, d_iters,
+                                                        d_conv, d_err);
+  } else {
+    ADT_CUDA(W.dirty.reserve((size_t)count * N));
+    k_eik2d_forward<false><<<count, thr, 0, stream>>>(cst, m, n, d_srcx, d_srcy, d_u,
+                                                      W.prev.as<double>(), W.dirty.as<uint8_t>(),
+                                                      d_iters, d_conv, d_err);
+  }
+  ADT_CUDA(cudaGetLastError());
+  std::vector<char> hs((size_t)count * (2 * sizeof(int) + sizeof(double)));
+  ADT_CUDA(cudaMemcpyAsync(hs.data(), W.stat.p, hs.size(), cudaMemcpyDeviceToHost, stream));
   ADT_CUDA(cudaStreamSynchronize(stream));
+  const double* er = reinterpret_cast<const double*>(hs.data());
+  const int* it = reinterpret_cast<const int*>(er + count);
+  const int* cv = it + count;
   if (st)
     for (int k = 0; k < count; ++k) {
       st[k].iters = it[k];
@@ -351,23 +466,33 @@ int eik2d_forward_batch(const double* d_f, int m, int n, double h, int count, co
 int eik2d_adjoint(const double* d_gu, const double* d_u, const double* d_f, int m, int n, double h,
                   int ix, int jx, double* d_gf, cudaStream_t stream) {
   const int64_t N = (int64_t)(m + 1) * (n + 1);
-  DevBuf lam, stat;
-  ADT_CUDA(lam.reserve((size_t)N * sizeof(double)));
-  ADT_CUDA(stat.reserve(sizeof(int)));
-  if (N < (1 << 30)) {  // causal order: every cell once
-    DevBuf word, queue;
-    ADT_CUDA(word.reserve((size_t)N * sizeof(uint32_t)));
-    ADT_CUDA(queue.reserve((size_t)N * sizeof(int)));
-    k_eik2d_adjoint_causal<<<1, 512, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, lam.as<double>(),
-                                                  d_gf, word.as<uint32_t>(), queue.as<int>(),
-                                                  stat.as<int>());
+  int dev = 0;
+  ADT_CUDA(cudaGetDevice(&dev));
+  Eik2dWork& W = work2d(dev);
+  std::lock_guard<std::mutex> lock(W.mu);
+  ADT_CUDA(W.lam.reserve((size_t)N * sizeof(double)));
+  ADT_CUDA(W.stat.reserve(sizeof(int)));
+  int* d_stat = W.stat.as<int>();
+  if (N <= ADJ2_SMEM_NODES) {  // causal order, working set in shared memory
+    const int smem = (int)(N * 12 + (N + 3) / 4 * 4);
+    ADT_CUDA(cudaFuncSetAttribute(k_eik2d_adjoint_causal<true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_eik2d_adjoint_causal<true><<<1, 512, smem, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx,
+                                                           nullptr, d_gf, nullptr, nullptr, d_stat);
+  } else if (N < (1 << 30)) {  // causal order: every cell once
+    ADT_CUDA(W.word.reserve((size_t)N * sizeof(uint32_t)));
+    ADT_CUDA(W.queue.reserve((size_t)N * sizeof(int)));
+    k_eik2d_adjoint_causal<false><<<1, 512, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx,
+                                                         W.lam.as<double>(), d_gf,
+                                                         W.word.as<uint32_t>(), W.queue.as<int>(),
+                                                         d_stat);
   } else {
-    k_eik2d_adjoint<<<1, 256, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, lam.as<double>(), d_gf,
-                                           stat.as<int>());
+    k_eik2d_adjoint<<<1, 256, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, W.lam.as<double>(),
+                                           d_gf, d_stat);
   }
   ADT_CUDA(cudaGetLastError());
   int s = 0;
-  ADT_CUDA(cudaMemcpyAsync(&s, stat.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  ADT_CUDA(cudaMemcpyAsync(&s, d_stat, sizeof(int), cudaMemcpyDeviceToHost, stream));
   ADT_CUDA(cudaStreamSynchronize(stream));
   if (s < 0) return set_error(ADT_ESINGULAR, "2D adjoint: a non-source cell has no upwind direction");
   if (s == 0) return set_error(ADT_ENOCONV, "2D adjoint did not complete");

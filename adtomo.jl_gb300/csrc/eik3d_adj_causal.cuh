@@ -145,11 +145,18 @@ __device__ __forceinline__ T causal_lambda(uint32_t mt, const T (&dc)[3], const 
 #pragma unroll
     for (int q = 0; q < 6; ++q)
       if (mt & (1u << (CODE_USERS + q))) acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(2.0, w[q]), ln[q]));
+    // d = 0 + t_x + t_y + t_z over the active axes; every t is positive, so
+    // the first addition (0 + t = t) is left out
     double d = 0.0;
+    bool any = false;
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax)
-      if ((mt >> (2 * ax)) & 3u) d = __dadd_rn(d, __dmul_rn(2.0, dc[ax]));
-    return __ddiv_rn(acc, d);
+      if ((mt >> (2 * ax)) & 3u) {
+        const double t = __dmul_rn(2.0, dc[ax]);
+        d = any ? __dadd_rn(d, t) : t;
+        any = true;
+      }
+    return fi_div(acc, d);
   }
 }
 

@@ -851,7 +851,7 @@ __device__ __forceinline__ bool sweep_brick_adj(const T* U, T* L, const uint16_t
               d += T(2) * (uc - uu);
           }
         }
-        const T lam = EXACT ? (T)__ddiv_rn((double)acc, (double)d) : acc / d;
+        const T lam = EXACT ? (T)fi_div((double)acc, (double)d) : acc / d;
         if (!(lam == L[a])) {
           L[a] = lam;
           changed = true;

@@ -16,6 +16,7 @@
 //    the travel time instead of losing digits to (a+b)^2 when u >> f h.
 #pragma once
 #include "adt_common.cuh"
+#include "fp64_int.cuh"
 
 namespace adt {
 
@@ -39,15 +40,17 @@ __device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, do
   return __dmul_rn(__dadd_rn(-B, __dsqrt_rn(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
 }
 
-// Two-term update, reference arithmetic (Eikonal.h:14-20).
-__device__ __forceinline__ double upd2_exact(double a, double b, double f, double h) {
-  const double fh = __dmul_rn(f, h);
+// Two-term update, reference arithmetic (Eikonal.h:14-20), given the node's
+// fh = f h and q2 = 2 f f h h (each formed in the reference's order).  The
+// square root runs on the integer pipes (fp64_int.cuh; the same bits as
+// __dsqrt_rn): the one-CTA 2D wavefront keeps four warps busy, where the FP64
+// unit, shared by the SM, serialises every FP64 instruction of the four.
+__device__ __forceinline__ double upd2_exact(double a, double b, double fh, double q2) {
   const double d = fabs(__dsub_rn(a, b));
   if (d >= fh) return __dadd_rn(rmin(a, b), fh);
   const double ab = __dsub_rn(a, b);
-  const double disc =
-      __dsub_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, f), f), h), h), __dmul_rn(ab, ab));
-  return __dmul_rn(__dadd_rn(__dadd_rn(a, b), __dsqrt_rn(disc)), 0.5);
+  const double disc = __dsub_rn(q2, __dmul_rn(ab, ab));
+  return __dmul_rn(__dadd_rn(__dadd_rn(a, b), fi_sqrt(disc)), 0.5);
 }
 
 template <class T>

@@ -169,6 +169,25 @@ def test_2d_c1_config_forward_and_grad():
     assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 1.0))
 
 
+@pytest.mark.parametrize("shape,src", [((140, 150), (3, 130)), ((161, 200), (150, 7))])
+def test_2d_grids_beyond_the_shared_memory_paths(shape, src):
+    """Grids of 21000 and 32200 nodes: the forward keeps its travel times and
+    change flags in shared memory up to 25600 nodes and the causal adjoint its
+    working set up to 17600, so these run the forward's shared-memory path
+    with the adjoint's global one, and both global paths.  Bit-identical to
+    the oracle, with the exact skipping of unchanged nodes in the forward."""
+    rng = np.random.default_rng(5)
+    f = rng.uniform(0.4, 1.6, size=shape)
+    jx, ix = src
+    u, st = A.eikonal(f, ix + 1, jx + 1, 0.3, return_status=True)
+    ur, it, conv = O.eik2d_forward(f, ix, jx, 0.3)
+    assert np.array_equal(u, ur) and st.iters == it and st.converged == conv
+    gu = np.zeros_like(u)
+    gu[rng.integers(0, shape[0], 40), rng.integers(0, shape[1], 40)] = rng.standard_normal(40)
+    gf = A.eikonal_grad(gu, u, f, ix + 1, jx + 1, 0.3)
+    assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 0.3))
+
+
 def test_2d_adjoint_singular_row_is_an_error():
     """A non-source cell with no upwind direction (u smaller than all four
     neighbours away from the source) leaves its adjoint row without a
