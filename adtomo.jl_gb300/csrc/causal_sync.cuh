@@ -27,24 +27,6 @@ __device__ __forceinline__ uint32_t atom_and_acq_rel_cta(uint32_t* p, uint32_t v
   return old;
 }
 
-// The same on shared memory.
-__device__ __forceinline__ int ld_acquire_cta_shared(const int* p) {
-  int v;
-  asm volatile("ld.acquire.cta.shared.b32 %0, [%1];"
-               : "=r"(v) : "r"((uint32_t)__cvta_generic_to_shared(p)) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_cta_shared(int* p, int v) {
-  asm volatile("st.release.cta.shared.b32 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(p)),
-               "r"(v) : "memory");
-}
-__device__ __forceinline__ uint32_t atom_and_acq_rel_cta_shared(uint32_t* p, uint32_t v) {
-  uint32_t old;
-  asm volatile("atom.acq_rel.cta.shared.and.b32 %0, [%1], %2;"
-               : "=r"(old) : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(v) : "memory");
-  return old;
-}
-
 // The lanes that arrive together take consecutive slots of a shared counter:
 // n (0..3) each; one shared atomic per group of lanes.  Callable from
 // divergent code (the group is __activemask()).

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 #include "eik2d.h"
 #include "eik3d_common_host.h"
@@ -50,9 +51,11 @@ __device__ __forceinline__ void ord2(int o, int& si, int& sj) {
 // Travel times and change flags of a solve stay in shared memory up to this
 // many nodes (9 bytes each).
 constexpr int FWD2_SMEM_NODES = 25600;
-// The causal adjoint's lambda, queue and flags stay in shared memory up to
-// this many nodes (13 bytes each).
+// The adjoint by levels keeps lambda, the queue and the flags in shared
+// memory up to ADJ2_SMEM_NODES nodes (13 bytes each), and the travel times
+// too, with a 16-bit queue, up to ADJ2_STAGE_U_NODES (19 bytes each).
 constexpr int ADJ2_SMEM_NODES = 17600;
+constexpr int ADJ2_STAGE_U_NODES = 12200;
 
 }  // namespace
 
@@ -246,60 +249,189 @@ __global__ void k_eik2d_adjoint(const double* __restrict__ gu, const double* __r
   if (threadIdx.x == 0) status[0] = s_singular ? -1 : (done ? it + 1 : 0);
 }
 
-// The 2D adjoint in causal order, one CTA: the rows of k_eik2d_adjoint
-// (Eikonal.h:95-200) solved once, every cell after its users (Kahn's
-// algorithm on the users graph, acyclic since a user's travel time is
-// strictly larger).  A cell's users are the non-source neighbours whose
-// upwind neighbour along the axis is the cell; per cell a flag set holds
-// their bits (x-, x+, y-, y+) and those not yet evaluated.  Each evaluated
-// non-source cell clears its bit in its upwind neighbours' sets (acq_rel
-// atomics at CTA scope); the thread that empties a set queues that cell
-// (release store; slots are read with acquire loads).  The per-cell formula
-// and summation order are k_eik2d_adjoint's, so lambda is the same, bit for
-// bit.  status: 1 done, -1 a non-source cell has no upwind direction, 0 a
-// wait on the queue ran out (bounded by CAUSAL_WAIT_CYCLES).
-//
-// SMEM (grids up to ADJ2_SMEM_NODES nodes): lambda, the queue and the flag
-// sets (one byte per cell: users in bits 0-3, outstanding in 4-7, four
-// cells to a 32-bit word for the atomics) live in dynamic shared memory, so
-// the dependent steps of the evaluation chain (queue slot, users' lambda,
-// release) stay on the SM.  Otherwise lam, word (one 32-bit set per cell:
-// users in bits 0-3, outstanding in 8-11) and queue are global.
-template <bool SMEM>
+// One row of the 2D adjoint (Eikonal.h:95-200) for cell x, whose users (bits
+// x-, x+, y-, y+ in us) are evaluated: lambda_x = (g_x + sum_users
+// 2 (u_r - u_x) lambda_r) / d_x, d_x = sum over the upwind axes of
+// 2 (u_x - u_upwind) (1 at the source), in k_eik2d_adjoint's order.  Also
+// returns the upwind neighbours (nx, ny) and which axes are upwind.
+__device__ __forceinline__ double adj2_row(const double* __restrict__ gu,
+                                           const double* __restrict__ u, const double* lam, int x,
+                                           uint32_t us, int m, int n, int src, int& nx, int& ny,
+                                           bool& ax, bool& ay) {
+  const int w = m + 1;
+  const int i = x % w, j = x / w;
+  double acc = gu[x];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if ((us >> q) & 1u) {
+      const int r = x + (q == 0 ? -1 : q == 1 ? 1 : q == 2 ? -w : w);
+      acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(2.0, __dsub_rn(u[r], u[x])), lam[r]));
+    }
+  nx = (int)upw2(u, x, i, m, 1);
+  ny = (int)upw2(u, x, j, n, w);
+  ax = x != src && u[x] > u[nx];
+  ay = x != src && u[x] > u[ny];
+  double d;
+  if (x == src) {
+    d = 1.0;
+  } else {
+    // 0 + t is t for the positive t of an upwind axis: the first term needs
+    // no addition
+    const double tx = ax ? __dmul_rn(2.0, __dsub_rn(u[x], u[nx])) : 0.0;
+    const double ty = ay ? __dmul_rn(2.0, __dsub_rn(u[x], u[ny])) : 0.0;
+    d = (ax && ay) ? __dadd_rn(tx, ty) : (ax ? tx : ty);
+  }
+  return fi_div(acc, d);
+}
+
+// Users of cell c (bits x-, x+, y-, y+): the non-source neighbours whose
+// upwind neighbour along the axis is c; singular: c is not the source and
+// has no upwind axis (its row has no diagonal).
+__device__ __forceinline__ uint32_t adj2_users(const double* __restrict__ u, int c, int m, int n,
+                                               int src, bool& singular) {
+  const int w = m + 1;
+  const int i = c % w, j = c / w;
+  uint32_t us = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int ri = i + (q == 0 ? -1 : q == 1 ? 1 : 0);
+    const int rj = j + (q == 2 ? -1 : q == 3 ? 1 : 0);
+    if (ri < 0 || ri > m || rj < 0 || rj > n) continue;
+    const int r = rj * w + ri;
+    if (r == src) continue;
+    const int64_t nb = (q < 2) ? upw2(u, r, ri, m, 1) : upw2(u, r, rj, n, w);
+    if (nb == c && u[r] > u[c]) us |= 1u << q;
+  }
+  singular = c != src && !(u[c] > u[upw2(u, c, i, m, 1)]) && !(u[c] > u[upw2(u, c, j, n, w)]);
+  return us;
+}
+
+// The 2D adjoint in causal order by levels, one CTA, for grids up to
+// ADJ2_SMEM_NODES nodes: the rows of k_eik2d_adjoint solved once, every cell
+// after its users (Kahn's algorithm on the users graph, acyclic since a
+// user's travel time is strictly larger), one level of the graph per round.
+// Round r evaluates the cells queued in round r - 1 (all their users are in
+// earlier rounds), clears their bits in their upwind neighbours' flag sets
+// and queues the neighbours whose sets empty; a barrier ends the round.
+// lambda, the queue and the flags (one byte per cell: users in bits 0-3, not
+// yet evaluated in 4-7, four cells to a 32-bit word for the atomics) live in
+// dynamic shared memory; with STAGE_U (grids up to ADJ2_STAGE_U_NODES
+// nodes) the travel times are copied there as well and the queue holds
+// 16-bit cell indices.  The formula and summation order are
+// k_eik2d_adjoint's, so lambda is the same, bit for bit.  No thread waits on
+// another except at the barriers; the rounds end when one queues nothing.
+// status: 1 done, -1 a non-source cell has no upwind direction, 0 cells left
+// unevaluated (impossible for travel times from the forward).
+template <bool STAGE_U>
+__global__ void __launch_bounds__(512)
+    k_eik2d_adjoint_levels(const double* __restrict__ gu, const double* __restrict__ u_g,
+                           const double* __restrict__ f, int m, int n, double h, int ix, int jx,
+                           double* __restrict__ grad_f, int* __restrict__ status) {
+  using QT = typename std::conditional<STAGE_U, uint16_t, int>::type;
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  __shared__ int s_cnt[3], s_singular;
+  const int w = m + 1;
+  const int N = (m + 1) * (n + 1);
+  const int src = jx * w + ix;
+  const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  double* lam = reinterpret_cast<double*>(adj_smem);
+  double* u_s = lam + N;
+  const double* u = STAGE_U ? u_s : u_g;
+  QT* queue = reinterpret_cast<QT*>(adj_smem + (size_t)N * (STAGE_U ? 16 : 8));
+  // 32-bit flag words after the queue, at a multiple of 4 bytes
+  uint32_t* word =
+      reinterpret_cast<uint32_t*>(adj_smem + ((size_t)N * (STAGE_U ? 18 : 12) + 3) / 4 * 4);
+  uint8_t* flag = reinterpret_cast<uint8_t*>(word);
+  if (tid == 0) {
+    s_cnt[0] = s_cnt[1] = s_cnt[2] = 0;
+    s_singular = 0;
+  }
+  if (STAGE_U)
+    for (int p = tid; p < N; p += nth) u_s[p] = u_g[p];
+  __syncthreads();
+  // level 0: the cells without users
+  for (int c0 = warp * 32; c0 < N; c0 += nth) {
+    const int c = c0 + lane;
+    uint32_t us = 0;
+    if (c < N) {
+      bool sing;
+      us = adj2_users(u, c, m, n, src, sing);
+      flag[c] = (uint8_t)(us | (us << 4));
+      if (sing) s_singular = 1;
+    }
+    const int pos = warp_append((c < N && us == 0) ? 1 : 0, &s_cnt[0], lane);
+    if (c < N && us == 0) queue[pos] = (QT)c;
+  }
+  __syncthreads();
+  int lo = 0, hi = s_cnt[0];
+  if (!s_singular) {
+    // round r appends to s_cnt[(r + 1) % 3]; thread 0 clears the counter of
+    // round r + 1 before the barrier ending round r (its last readers passed
+    // the barrier ending round r - 1)
+    for (int r = 0; lo < hi; ++r) {
+      int* cnt = &s_cnt[(r + 1) % 3];
+      if (tid == 0) s_cnt[(r + 2) % 3] = 0;
+      for (int k0 = lo; k0 < hi; k0 += nth) {
+        const int k = k0 + tid;
+        int rel[2] = {-1, -1}, np = 0;
+        if (k < hi) {
+          const int x = queue[k];
+          int nx, ny;
+          bool ax, ay;
+          lam[x] = adj2_row(gu, u, lam, x, flag[x] & 15u, m, n, src, nx, ny, ax, ay);
+          // release the upwind neighbours this cell is a user of: x+ (1)
+          // or x- (0) seen from nx, y+ (3) or y- (2) seen from ny
+          const int nbs[2] = {nx, ny};
+          const bool act[2] = {ax, ay};
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            if (!act[a]) continue;
+            const int nb = nbs[a];
+            const int q = a == 0 ? (nb < x ? 1 : 0) : (nb < x ? 3 : 2);
+            const int sh = 8 * (nb & 3);
+            const uint32_t bit = (1u << (q + 4)) << sh;
+            const uint32_t old = atomicAnd(word + (nb >> 2), ~bit);
+            if ((old & bit) && !(old & ~bit & (0xf0u << sh))) rel[a] = nb, ++np;
+          }
+        }
+        const int pos = hi + warp_append(np, cnt, lane);
+        int o = pos;
+        for (int a = 0; a < 2; ++a)
+          if (rel[a] >= 0) queue[o++] = (QT)rel[a];
+      }
+      __syncthreads();
+      lo = hi;
+      hi += *cnt;
+    }
+  }
+  __syncthreads();
+  const bool done = !s_singular && hi == N;
+  for (int p = tid; p < N; p += nth) {
+    // dFdf = -2 f h h, 0 at the source; grad_f = -lambda * dFdf (Eikonal.h:100-104,196-198)
+    const double dfdf = (p == src) ? 0.0 : __dmul_rn(__dmul_rn(__dmul_rn(-2.0, f[p]), h), h);
+    grad_f[p] = done ? __dmul_rn(-lam[p], dfdf) : 0.0;
+  }
+  if (tid == 0) status[0] = s_singular ? -1 : (done ? 1 : 0);
+}
+
+// The 2D adjoint in causal order for larger grids, one CTA, without
+// barriers: threads take queue slots and wait for their cells (bounded by
+// CAUSAL_WAIT_CYCLES); lambda, the queue and the flag sets (one 32-bit word
+// per cell: users in bits 0-3, not yet evaluated in 8-11) are global.  Each
+// evaluated non-source cell clears its bit in its upwind neighbours' sets
+// (acq_rel atomics at CTA scope); the thread that empties a set queues that
+// cell (release store; slots are read with acquire loads).  status as
+// k_eik2d_adjoint_levels, 0 also when a wait ran out.
 __global__ void __launch_bounds__(512)
     k_eik2d_adjoint_causal(const double* __restrict__ gu, const double* __restrict__ u,
                            const double* __restrict__ f, int m, int n, double h, int ix, int jx,
-                           double* lam_g, double* __restrict__ grad_f, uint32_t* word_g,
-                           int* queue_g, int* __restrict__ status) {
-  extern __shared__ __align__(16) unsigned char adj_smem[];
+                           double* lam, double* __restrict__ grad_f, uint32_t* word, int* queue,
+                           int* __restrict__ status) {
   __shared__ int s_head, s_tail, s_err, s_singular;
   const int w = m + 1;
   const int N = (m + 1) * (n + 1);
   const int src = jx * w + ix;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  double* lam = SMEM ? reinterpret_cast<double*>(adj_smem) : lam_g;
-  int* queue = SMEM ? reinterpret_cast<int*>(adj_smem + (size_t)N * 8) : queue_g;
-  uint32_t* word = SMEM ? reinterpret_cast<uint32_t*>(adj_smem + (size_t)N * 12) : word_g;
-  uint8_t* flag = reinterpret_cast<uint8_t*>(word);
-  auto q_load = [&](int slot) {
-    return SMEM ? ld_acquire_cta_shared(queue + slot) : ld_acquire_cta(queue + slot);
-  };
-  auto q_store = [&](int slot, int v) {
-    if (SMEM) st_release_cta_shared(queue + slot, v);
-    else st_release_cta(queue + slot, v);
-  };
-  // clears user bit q of cell nb; true when that emptied its outstanding set
-  auto release = [&](int nb, int q) -> bool {
-    if (SMEM) {
-      const int sh = 8 * (nb & 3);
-      const uint32_t bit = (1u << (q + 4)) << sh;
-      const uint32_t old = atom_and_acq_rel_cta_shared(word + (nb >> 2), ~bit);
-      return (old & bit) && !(old & ~bit & (0xf0u << sh));
-    }
-    const uint32_t bit = (1u << q) << 8;
-    const uint32_t old = atom_and_acq_rel_cta(word + nb, ~bit);
-    return (old & bit) && !(old & ~bit & 0xf00u);
-  };
   if (tid == 0) {
     s_head = s_tail = 0;
     s_err = s_singular = 0;
@@ -311,21 +443,10 @@ __global__ void __launch_bounds__(512)
     const int c = c0 + lane;
     uint32_t us = 0;
     if (c < N) {
-      const int i = c % w, j = c / w;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int ri = i + (q == 0 ? -1 : q == 1 ? 1 : 0);
-        const int rj = j + (q == 2 ? -1 : q == 3 ? 1 : 0);
-        if (ri < 0 || ri > m || rj < 0 || rj > n) continue;
-        const int r = rj * w + ri;
-        if (r == src) continue;
-        const int64_t nb = (q < 2) ? upw2(u, r, ri, m, 1) : upw2(u, r, rj, n, w);
-        if (nb == c && u[r] > u[c]) us |= 1u << q;
-      }
-      if (SMEM) flag[c] = (uint8_t)(us | (us << 4));
-      else word[c] = us | (us << 8);
-      if (c != src && !(u[c] > u[upw2(u, c, i, m, 1)]) && !(u[c] > u[upw2(u, c, j, n, w)]))
-        s_singular = 1;
+      bool sing;
+      us = adj2_users(u, c, m, n, src, sing);
+      word[c] = us | (us << 8);
+      if (sing) s_singular = 1;
     }
     const int pos = warp_append((c < N && us == 0) ? 1 : 0, &s_tail, lane);
     if (c < N && us == 0) queue[pos] = c;
@@ -335,12 +456,12 @@ __global__ void __launch_bounds__(512)
     for (;;) {
       const int slot = take_slots(1, &s_head);
       if (slot >= N) break;
-      int x = q_load(slot);
+      int x = ld_acquire_cta(queue + slot);
       if (x < 0) {
         const long long t0 = clock64();
         do {
           __nanosleep(64);
-          x = q_load(slot);
+          x = ld_acquire_cta(queue + slot);
         } while (x < 0 && clock64() - t0 < CAUSAL_WAIT_CYCLES &&
                  !*reinterpret_cast<volatile int*>(&s_err));
         if (x < 0) {  // out of budget, or another thread's was
@@ -348,47 +469,29 @@ __global__ void __launch_bounds__(512)
           break;
         }
       }
-      const int i = x % w, j = x / w;
-      const uint32_t us = (SMEM ? (uint32_t)flag[x] : word[x]) & 15u;
-      double acc = gu[x];
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if ((us >> q) & 1u) {
-          const int r = x + (q == 0 ? -1 : q == 1 ? 1 : q == 2 ? -w : w);
-          acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(2.0, __dsub_rn(u[r], u[x])), lam[r]));
-        }
-      double d;
-      const int nx = (int)upw2(u, x, i, m, 1), ny = (int)upw2(u, x, j, n, w);
-      if (x == src) {
-        d = 1.0;
-      } else {
-        // 0 + t is t for the positive t of an upwind axis: the first term
-        // needs no addition
-        const bool ax = u[x] > u[nx], ay = u[x] > u[ny];
-        const double tx = ax ? __dmul_rn(2.0, __dsub_rn(u[x], u[nx])) : 0.0;
-        const double ty = ay ? __dmul_rn(2.0, __dsub_rn(u[x], u[ny])) : 0.0;
-        d = (ax && ay) ? __dadd_rn(tx, ty) : (ax ? tx : ty);
-      }
-      lam[x] = fi_div(acc, d);
+      int nx, ny;
+      bool ax, ay;
+      lam[x] = adj2_row(gu, u, lam, x, word[x] & 15u, m, n, src, nx, ny, ax, ay);
       // release the upwind neighbours this cell is a user of
       int rel[2] = {-1, -1}, np = 0;
-      if (x != src) {
-        const int nbs[2] = {nx, ny};
+      const int nbs[2] = {nx, ny};
+      const bool act[2] = {ax, ay};
 #pragma unroll
-        for (int a = 0; a < 2; ++a) {
-          const int nb = nbs[a];
-          if (!(u[x] > u[nb])) continue;
-          // this cell seen from nb: x+ (1) or x- (0), y+ (3) or y- (2)
-          const int q = a == 0 ? (nb < x ? 1 : 0) : (nb < x ? 3 : 2);
-          if (release(nb, q)) {
-            rel[a] = nb;
-            ++np;
-          }
+      for (int a = 0; a < 2; ++a) {
+        if (!act[a]) continue;
+        const int nb = nbs[a];
+        // this cell seen from nb: x+ (1) or x- (0), y+ (3) or y- (2)
+        const int q = a == 0 ? (nb < x ? 1 : 0) : (nb < x ? 3 : 2);
+        const uint32_t bit = (1u << q) << 8;
+        const uint32_t old = atom_and_acq_rel_cta(word + nb, ~bit);
+        if ((old & bit) && !(old & ~bit & 0xf00u)) {
+          rel[a] = nb;
+          ++np;
         }
       }
       int pos = take_slots(np, &s_tail);
       for (int a = 0; a < 2; ++a)
-        if (rel[a] >= 0) q_store(pos++, rel[a]);
+        if (rel[a] >= 0) st_release_cta(queue + pos++, rel[a]);
     }
   }
   __syncthreads();
@@ -473,19 +576,24 @@ int eik2d_adjoint(const double* d_gu, const double* d_u, const double* d_f, int 
   ADT_CUDA(W.lam.reserve((size_t)N * sizeof(double)));
   ADT_CUDA(W.stat.reserve(sizeof(int)));
   int* d_stat = W.stat.as<int>();
-  if (N <= ADJ2_SMEM_NODES) {  // causal order, working set in shared memory
-    const int smem = (int)(N * 12 + (N + 3) / 4 * 4);
-    ADT_CUDA(cudaFuncSetAttribute(k_eik2d_adjoint_causal<true>,
+  if (N <= ADJ2_STAGE_U_NODES) {  // causal order by levels, travel times staged
+    const int smem = (int)((N * 18 + 3) / 4 * 4 + (N + 3) / 4 * 4);
+    ADT_CUDA(cudaFuncSetAttribute(k_eik2d_adjoint_levels<true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    k_eik2d_adjoint_causal<true><<<1, 512, smem, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx,
-                                                           nullptr, d_gf, nullptr, nullptr, d_stat);
+    k_eik2d_adjoint_levels<true><<<1, 256, smem, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, d_gf,
+                                                           d_stat);
+  } else if (N <= ADJ2_SMEM_NODES) {  // causal order by levels
+    const int smem = (int)(N * 12 + (N + 3) / 4 * 4);
+    ADT_CUDA(cudaFuncSetAttribute(k_eik2d_adjoint_levels<false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_eik2d_adjoint_levels<false><<<1, 256, smem, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, d_gf,
+                                                            d_stat);
   } else if (N < (1 << 30)) {  // causal order: every cell once
     ADT_CUDA(W.word.reserve((size_t)N * sizeof(uint32_t)));
     ADT_CUDA(W.queue.reserve((size_t)N * sizeof(int)));
-    k_eik2d_adjoint_causal<false><<<1, 512, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx,
-                                                         W.lam.as<double>(), d_gf,
-                                                         W.word.as<uint32_t>(), W.queue.as<int>(),
-                                                         d_stat);
+    k_eik2d_adjoint_causal<<<1, 512, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx,
+                                                  W.lam.as<double>(), d_gf, W.word.as<uint32_t>(),
+                                                  W.queue.as<int>(), d_stat);
   } else {
     k_eik2d_adjoint<<<1, 256, 0, stream>>>(d_gu, d_u, d_f, m, n, h, ix, jx, W.lam.as<double>(),
                                            d_gf, d_stat);
