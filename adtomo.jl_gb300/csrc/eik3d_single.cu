@@ -22,7 +22,8 @@
 namespace adt {
 
 __global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f, Geom g,
-                            const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h) {
+                            const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h,
+                            int* __restrict__ stamps, int t) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q = blockIdx.x * (blockDim.x >> 5) + warp;
@@ -33,6 +34,19 @@ __global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f
   ordering3(o, si, sj, sk);
   const int CS = tile_col_stride(SBK, sj == sk);
   const BrickPos p = brick_pos<SBK>(g, bricks[q0 + q], si, sj, sk);
+  const int id = (p.bx * g.nby + p.by) * g.nbz + p.bz;
+  if (stamps) {  // exact brick skipping
+    const int swept = stamps[2 * id];
+    bool dirty = stamps[2 * id + 1] >= swept;
+    auto newer = [&](int x, int y, int z) { return stamps[2 * ((x * g.nby + y) * g.nbz + z) + 1] > swept; };
+    dirty = dirty || (p.bx > 0 && newer(p.bx - 1, p.by, p.bz)) ||
+            (p.bx < g.nbx - 1 && newer(p.bx + 1, p.by, p.bz)) ||
+            (p.by > 0 && newer(p.bx, p.by - 1, p.bz)) ||
+            (p.by < g.nby - 1 && newer(p.bx, p.by + 1, p.bz)) ||
+            (p.bz > 0 && newer(p.bx, p.by, p.bz - 1)) ||
+            (p.bz < g.nbz - 1 && newer(p.bx, p.by, p.bz + 1));
+    if (!dirty) return;
+  }
   load_halo_tile<double, SBK>(S, u, g, p, CS, lane);
   load_interior<double, SBK>(F, f, g, p, CS, lane);
   cp_async_wait_all();
@@ -42,6 +56,10 @@ __global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f
   const bool ch =
       sweep_brick_fwd<double, SBK, MODE_EXACT>(S, F, g, p, si, sj, sk, CS, h, h, nb, false, lane, md);
   if (ch) store_interior<double, SBK>(S, u, g, p, CS, lane);
+  if (stamps && lane == 0) {
+    stamps[2 * id] = t;
+    if (ch) stamps[2 * id + 1] = t;
+  }
 }
 
 // max |a - b| as the bit pattern of a non-negative double.
@@ -194,6 +212,7 @@ namespace {
 struct SingleWork {
   std::mutex mu;
   DevBuf uold, lam, code1, code, levels, scalar;
+  DevBuf stamps;  // forward brick skipping: per brick, last sweep and last change
   DevBuf meta, rec, queue;  // causal-order adjoint
   int lev_m = -1, lev_n = -1, lev_l = -1;
   LevelList host_levels;
@@ -235,6 +254,9 @@ int eik3d_single_forward(const double* d_u0, const double* d_f, double h, int m,
   if (rc) return rc;
   ADT_CUDA(W.uold.reserve(bytes));
   ADT_CUDA(W.scalar.reserve(sizeof(unsigned long long)));
+  const int64_t nbricks = (int64_t)g.nbx * g.nby * g.nbz;
+  ADT_CUDA(W.stamps.reserve((size_t)nbricks * 2 * sizeof(int)));
+  ADT_CUDA(cudaMemsetAsync(W.stamps.p, 0, (size_t)nbricks * 2 * sizeof(int), stream));
   static bool attr_set[64] = {false};
   if (!attr_set[dev & 63]) {
     ADT_CUDA(cudaFuncSetAttribute(k_level_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -255,8 +277,8 @@ int eik3d_single_forward(const double* d_u0, const double* d_f, double h, int m,
       for (int d = 0; d < g.nlev; ++d) {
         const int cnt = start[d + 1] - start[d];
         const int blocks = (cnt + FWD_WPB - 1) / FWD_WPB;
-        k_level_fwd<<<blocks, FWD_WPB * 32, FWD_WPB * FWD_WARP_SMEM, stream>>>(d_u, d_f, g, lv,
-                                                                               start[d], cnt, o, h);
+        k_level_fwd<<<blocks, FWD_WPB * 32, FWD_WPB * FWD_WARP_SMEM, stream>>>(
+            d_u, d_f, g, lv, start[d], cnt, o, h, W.stamps.as<int>(), 1 + (it * 8 + o) * g.nlev + d);
       }
     ADT_CUDA(cudaGetLastError());
     ADT_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned long long), stream));

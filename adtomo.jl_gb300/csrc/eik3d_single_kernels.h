@@ -14,9 +14,16 @@ constexpr size_t FWD_WARP_SMEM = (tile_elems(SBK) + itile_elems(SBK)) * sizeof(d
 constexpr size_t ADJ_WARP_SMEM =
     (2 * tile_elems(SBK) + itile_elems(SBK)) * sizeof(double) + itile_elems(SBK) * sizeof(uint16_t);
 
-// One level of one ordering: one warp per brick of the level.
+// One level of one ordering: one warp per brick of the level.  With stamps
+// (per brick: the time of its last sweep, then of its last change; zeros at
+// the start) a brick is swept only if its last sweep changed it or a face
+// neighbour changed after that sweep: otherwise every cell already satisfies
+// its update and a sweep would change nothing (exact).  t: this launch's
+// time, larger than any before it; the bricks of one level are not face
+// neighbours, so no stamp is read and written by the same launch.
 __global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f, Geom g,
-                            const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h);
+                            const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h,
+                            int* __restrict__ stamps, int t);
 // max |a - b| as the bit pattern of a non-negative double (atomicMax into *out).
 __global__ void k_maxdiff(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
                           unsigned long long* out);
