@@ -9,8 +9,8 @@
 //    correctly rounded value of the same exact quotient, so the bits are the
 //    same, and the multiplication is one instruction where the division is a
 //    long dependent sequence in FP64.  Square roots and the divisions by 3
-//    run on the integer pipes (fi_sqrt, fi_div in fp64_int.cuh: the same bits,
-//    a shorter chain and a fraction of the FP64 unit's time).
+//    run on the integer pipes (fi_sqrt, fi_div3 in fp64_int.cuh: the same
+//    bits, a shorter chain and a fraction of the FP64 unit's time).
 //  * upd3_stable<T>: the same roots written without the B^2 - 4C cancellation:
 //      two-term:   x = a + (d2 + sqrt(2 F^2 - d2^2)) / 2,           d2 = b - a
 //      three-term: x = a + (d2 + d3 + sqrt(3 F^2 - d2^2 - d3^2 - (d3-d2)^2)) / 3
@@ -35,10 +35,9 @@ __device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, do
   double C = __dmul_rn(__dsub_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), ffhh), 0.5);
   x = __dmul_rn(__dadd_rn(-B, fi_sqrt(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
   if (x <= a3) return x;
-  B = fi_div(__dmul_rn(-2.0, __dadd_rn(__dadd_rn(a1, a2), a3)), 3.0);
-  C = fi_div(
-      __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), __dmul_rn(a3, a3)), ffhh),
-      3.0);
+  B = fi_div3(__dmul_rn(-2.0, __dadd_rn(__dadd_rn(a1, a2), a3)));
+  C = fi_div3(
+      __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), __dmul_rn(a3, a3)), ffhh));
   return __dmul_rn(__dadd_rn(-B, fi_sqrt(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
 }
 

@@ -264,6 +264,27 @@ FI_HD double fi_div_core(uint64_t ab, uint64_t bb, float r0f) {
   return fi_double(sg | (((uint64_t)(biased - 1) << 52) + qi));
 }
 
+// a / 3, correctly rounded.  For a = m 2^E (m the 53-bit significand) the
+// 53-bit quotient is floor(m 2^k / 3), k = 1 when m >= 1.5 * 2^52, else 2:
+// an exact integer division by 3 (multiply-high by 0xAAAAAAAAAAAAAAAB, then
+// a shift, exact for every 64-bit dividend), whose remainder (0, 1 or 2)
+// decides the rounding: 2/3 of a unit rounds up, 1/3 down, no ties.
+FI_HD double fi_div3(double a) {
+  const uint64_t b = fi_bits(a);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  const uint64_t m = (b & FI_FRAC) | FI_HID;
+  const int k = m >= (3ull << 51) ? 1 : 2;
+  if (e - 1u >= 2046u || (int)e - k < 1) {
+    if ((b << 1) == 0) return a;  // +-0 / 3
+    return fi_hw_div(a, 3.0);     // subnormal, inf, NaN, or a subnormal quotient
+  }
+  const uint64_t n = m << k;
+  uint64_t q = fi_mulhi(n, 0xAAAAAAAAAAAAAAABull) >> 1;  // floor(n / 3)
+  q += (n - 3 * q == 2) ? 1u : 0u;
+  // a / 3 = q 2^(E - k): exponent field e - k (q carries into it at 2^53)
+  return fi_double((b & FI_SIGN) | (((uint64_t)(e - k - 1) << 52) + q));
+}
+
 FI_HD double fi_div(double a, double b) {
   const uint64_t ab = fi_bits(a), bb = fi_bits(b);
   const uint32_t ea = (uint32_t)(ab >> 52) & 0x7ffu, eb = (uint32_t)(bb >> 52) & 0x7ffu;

@@ -41,7 +41,7 @@ double div_seeded(double a, double b, double perturb) {
 }  // namespace
 
 // op: 0 sqrt(a), 1 a / b, 2 a < b, 3 a <= b, 4 a == b, 5 min(a, b),
-//     6 a*4, 7 a*2, 8 a*0.5, 9 a*0.25, 10 |a|
+//     6 a*4, 7 a*2, 8 a*0.5, 9 a*0.25, 10 |a|, 11 a / 3
 extern "C" int fi_check_run(int op, const double* a, const double* b, double* out, int64_t n,
                             double perturb) {
   for (int64_t i = 0; i < n; ++i) {
@@ -58,6 +58,7 @@ extern "C" int fi_check_run(int op, const double* a, const double* b, double* ou
       case 8: r = fi_scale<-1>(a[i]); break;
       case 9: r = fi_scale<-2>(a[i]); break;
       case 10: r = fi_abs(a[i]); break;
+      case 11: r = fi_div3(a[i]); break;
       default: return -1;
     }
     out[i] = r;

@@ -1,6 +1,6 @@
 """The integer-pipe FP64 operations (fp64_int.cuh) built for the host, against
-IEEE binary64 arithmetic, bit for bit: square root, division, compares, min,
-power-of-two scalings and |x|, on random operands over the whole exponent
+IEEE binary64 arithmetic, bit for bit: square root, division (and by 3),
+compares, min, power-of-two scalings and |x|, on random operands over the whole exponent
 range, on the travel-time range the solvers see, on the hard cases of each
 operation (neighbours of exact squares and exact quotients, mantissa
 extremes) and on zeros, subnormals, infinities and NaN (which take the
@@ -111,6 +111,21 @@ def test_sqrt_bit_exact(lib, perturb):
     with np.errstate(invalid="ignore"):
         want = np.sqrt(x)
     bad = same_bits(run(lib, 0, x, perturb=perturb), want)
+    assert bad.size == 0, f"{bad.size} mismatches, first x={x[bad[:5]]!r}"
+
+
+def test_div3_bit_exact(lib):
+    rng = np.random.default_rng(15)
+    n = 400000
+    s = specials()
+    x = np.concatenate([random_doubles(rng, n, 0, 2047, sign=True), rng.uniform(0, 1e5, n),
+                        3.0 * random_doubles(rng, n, 2, 2040), s, -s,
+                        from_bits(np.arange(1 << 52, (1 << 52) + 4096, dtype=np.uint64)),
+                        from_bits((np.uint64(1) << np.uint64(52)) * np.arange(1, 5, dtype=np.uint64)
+                                  | np.uint64((1 << 52) - 1))])
+    with np.errstate(all="ignore"):
+        want = x / 3.0
+    bad = same_bits(run(lib, 11, x), want)
     assert bad.size == 0, f"{bad.size} mismatches, first x={x[bad[:5]]!r}"
 
 
