@@ -188,6 +188,37 @@ def test_2d_grids_beyond_the_shared_memory_paths(shape, src):
     assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 0.3))
 
 
+@pytest.mark.parametrize("src", [(0, 0), (36, 52), (0, 52), (36, 0), (18, 0), (0, 26)])
+def test_2d_sources_on_corners_and_edges(src):
+    """Sources on the grid's corners and edges: the one-sided neighbour rule
+    (Eikonal.h:14-20 callers) through the forward's exact skipping and the
+    adjoint by levels, bit-identical to the oracle."""
+    rng = np.random.default_rng(6)
+    f = rng.uniform(0.5, 1.5, size=(37, 53))
+    jx, ix = src
+    u, st = A.eikonal(f, ix + 1, jx + 1, 0.5, return_status=True)
+    ur, it, conv = O.eik2d_forward(f, ix, jx, 0.5)
+    assert np.array_equal(u, ur) and st.iters == it and st.converged == conv
+    gu = np.zeros_like(u)
+    gu[rng.integers(0, 37, 12), rng.integers(0, 53, 12)] = rng.standard_normal(12)
+    gf = A.eikonal_grad(gu, u, f, ix + 1, jx + 1, 0.5)
+    assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 0.5))
+
+
+def test_2d_batch_beyond_shared_memory():
+    """Several sources on a 32200-node grid: the forward's global-memory path
+    with a change-flag array per solve."""
+    rng = np.random.default_rng(7)
+    f = rng.uniform(0.5, 1.5, size=(161, 200))
+    sx = rng.integers(1, 201, size=3)
+    sy = rng.integers(1, 162, size=3)
+    u, st = A.eikonal_batch(f, sx, sy, 0.4)
+    for k in range(3):
+        ur, it, conv = O.eik2d_forward(f, sx[k] - 1, sy[k] - 1, 0.4)
+        assert np.array_equal(u[k], ur)
+        assert st[k] == (it, int(conv))
+
+
 def test_2d_adjoint_singular_row_is_an_error():
     """A non-source cell with no upwind direction (u smaller than all four
     neighbours away from the source) leaves its adjoint row without a
