@@ -7,13 +7,18 @@
 // the Gauss-Seidel data flow of the reference's i-outer / j-inner loop, so
 // travel times are bit-identical.  The source cell is skipped and pinned to 0.
 // Stop when ||u - u_old|| / ||u_old|| < 1e-8, at most 100 iterations
-// (Eikonal.h:71-86).
+// (Eikonal.h:71-86).  Nodes none of whose neighbours changed since their last
+// update are skipped (exact); the travel times and those change flags live in
+// shared memory for grids up to FWD2_SMEM_NODES nodes.
 //
 // Adjoint (Eikonal.h:95-200): lambda_c = (g_c + sum_users 2 (u_r - u_c)
-// lambda_r) / d_c with the source row the identity, solved by the same
-// diagonal sweeps until a full iteration changes nothing.  A non-source cell
-// without an active axis makes the reference's matrix singular; it is
-// reported as ADT_ESINGULAR.
+// lambda_r) / d_c with the source row the identity.  The system is
+// triangular in travel-time order, so each row is solved once, after its
+// users: level by level in shared memory (k_eik2d_adjoint_levels), with a
+// queue in global memory for larger grids (k_eik2d_adjoint_causal), and by
+// the same diagonal sweeps until a full iteration changes nothing above 2^30
+// nodes (k_eik2d_adjoint).  A non-source cell without an active axis makes
+// the reference's matrix singular; it is reported as ADT_ESINGULAR.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
