@@ -140,7 +140,9 @@ struct NearBox {
   }
 };
 
-enum SweepMode { MODE_EXACT = 0, MODE_STABLE = 1 };
+// MODE_EXACT_CST: the exact update with F holding f h per cell and the next
+// interior tile (F + itile_elems(BK)) f f h h.
+enum SweepMode { MODE_EXACT = 0, MODE_STABLE = 1, MODE_EXACT_CST = 2 };
 
 // Forward sweep of one staged brick.  Returns the per-lane largest decrease
 // and whether any cell changed (any lane).
@@ -180,6 +182,9 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
       T un;
       if (MODE == MODE_EXACT) {
         un = (T)upd3_exact((double)ax, (double)ay, (double)az, (double)fc, hd);
+      } else if (MODE == MODE_EXACT_CST) {
+        un = (T)upd3_exact_fh((double)ax, (double)ay, (double)az, (double)fc,
+                              (double)F[fo + k + itile_elems(BK)]);
       } else {
         if (near && nb.has(i, j, kg))
           un = (T)upd3_stable<double>((double)ax, (double)ay, (double)az, (double)fc * hd);

@@ -115,7 +115,7 @@ int na_solve(NoAllocDevice& D, const double* u0, const double* f, double h, cons
       for (int d = 0; d < g.nlev; ++d) {
         const int cnt = D.start[d + 1] - D.start[d];
         k_level_fwd<<<(cnt + FWD_WPB - 1) / FWD_WPB, FWD_WPB * 32, FWD_WPB * FWD_WARP_SMEM, st>>>(
-            u, f, g, bricks, D.start[d], cnt, o, h, nullptr, 0);
+            u, f, nullptr, g, bricks, D.start[d], cnt, o, h, nullptr, 0);
       }
     ADT_CUDA(cudaGetLastError());
     ADT_CUDA(cudaMemsetAsync(err_word, 0, sizeof(unsigned long long), st));

@@ -21,7 +21,18 @@
 
 namespace adt {
 
-__global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f, Geom g,
+__global__ void k_fwd_cells(const double* __restrict__ f, double h, int64_t ncell,
+                            double* __restrict__ fcst) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double fv = f[c];
+    fcst[c] = __dmul_rn(fv, h);
+    fcst[ncell + c] = __dmul_rn(__dmul_rn(__dmul_rn(fv, fv), h), h);
+  }
+}
+
+__global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f,
+                            const double* __restrict__ fcst, Geom g,
                             const uint32_t* __restrict__ bricks, int q0, int cnt, int o, double h,
                             int* __restrict__ stamps, int t) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -48,13 +59,21 @@ __global__ void k_level_fwd(double* __restrict__ u, const double* __restrict__ f
     if (!dirty) return;
   }
   load_halo_tile<double, SBK>(S, u, g, p, CS, lane);
-  load_interior<double, SBK>(F, f, g, p, CS, lane);
+  if (fcst) {
+    load_interior<double, SBK>(F, fcst, g, p, CS, lane);
+    load_interior<double, SBK>(F + itile_elems(SBK), fcst + g.ncell, g, p, CS, lane);
+  } else {
+    load_interior<double, SBK>(F, f, g, p, CS, lane);
+  }
   cp_async_wait_all();
   __syncwarp();
   double md = 0.0;
   NearBox nb{1, 0, 1, 0, 1, 0};
   const bool ch =
-      sweep_brick_fwd<double, SBK, MODE_EXACT>(S, F, g, p, si, sj, sk, CS, h, h, nb, false, lane, md);
+      fcst ? sweep_brick_fwd<double, SBK, MODE_EXACT_CST>(S, F, g, p, si, sj, sk, CS, h, h, nb,
+                                                          false, lane, md)
+           : sweep_brick_fwd<double, SBK, MODE_EXACT>(S, F, g, p, si, sj, sk, CS, h, h, nb, false,
+                                                      lane, md);
   if (ch) store_interior<double, SBK>(S, u, g, p, CS, lane);
   if (stamps && lane == 0) {
     stamps[2 * id] = t;
@@ -213,6 +232,7 @@ struct SingleWork {
   std::mutex mu;
   DevBuf uold, lam, code1, code, levels, scalar;
   DevBuf stamps;  // forward brick skipping: per brick, last sweep and last change
+  DevBuf fcst;    // forward: f h and f f h h per cell
   DevBuf meta, rec, queue;  // causal-order adjoint
   int lev_m = -1, lev_n = -1, lev_l = -1;
   LevelList host_levels;
@@ -257,6 +277,8 @@ int eik3d_single_forward(const double* d_u0, const double* d_f, double h, int m,
   const int64_t nbricks = (int64_t)g.nbx * g.nby * g.nbz;
   ADT_CUDA(W.stamps.reserve((size_t)nbricks * 2 * sizeof(int)));
   ADT_CUDA(cudaMemsetAsync(W.stamps.p, 0, (size_t)nbricks * 2 * sizeof(int), stream));
+  ADT_CUDA(W.fcst.reserve(2 * bytes));
+  k_fwd_cells<<<grid_for(g.ncell), 256, 0, stream>>>(d_f, h, g.ncell, W.fcst.as<double>());
   static bool attr_set[64] = {false};
   if (!attr_set[dev & 63]) {
     ADT_CUDA(cudaFuncSetAttribute(k_level_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -278,7 +300,8 @@ int eik3d_single_forward(const double* d_u0, const double* d_f, double h, int m,
         const int cnt = start[d + 1] - start[d];
         const int blocks = (cnt + FWD_WPB - 1) / FWD_WPB;
         k_level_fwd<<<blocks, FWD_WPB * 32, FWD_WPB * FWD_WARP_SMEM, stream>>>(
-            d_u, d_f, g, lv, start[d], cnt, o, h, W.stamps.as<int>(), 1 + (it * 8 + o) * g.nlev + d);
+            d_u, d_f, W.fcst.as<double>(), g, lv, start[d], cnt, o, h, W.stamps.as<int>(),
+            1 + (it * 8 + o) * g.nlev + d);
       }
     ADT_CUDA(cudaGetLastError());
     ADT_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned long long), stream));

@@ -22,15 +22,19 @@
 
 namespace adt {
 
-// Sorted three-term update, reference arithmetic (Eikonal3D.cpp:11-28).
-__device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, double f, double h) {
+// Sorted three-term update, reference arithmetic (Eikonal3D.cpp:11-28), with
+// fh = f h given and ffhh = f f h h formed by ffhh_of() when the two-axis
+// root is needed.
+template <class FF>
+__device__ __forceinline__ double upd3_exact_core(double a1, double a2, double a3, double fh,
+                                                  FF ffhh_of) {
   double t;
   if (a1 > a2) { t = a1; a1 = a2; a2 = t; }
   if (a1 > a3) { t = a1; a1 = a3; a3 = t; }
   if (a2 > a3) { t = a2; a2 = a3; a3 = t; }
-  double x = __dadd_rn(a1, __dmul_rn(f, h));
+  double x = __dadd_rn(a1, fh);
   if (x <= a2) return x;
-  const double ffhh = __dmul_rn(__dmul_rn(__dmul_rn(f, f), h), h);
+  const double ffhh = ffhh_of();
   double B = -__dadd_rn(a1, a2);
   double C = __dmul_rn(__dsub_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), ffhh), 0.5);
   x = __dmul_rn(__dadd_rn(-B, fi_sqrt(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
@@ -39,6 +43,19 @@ __device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, do
   C = fi_div3(
       __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), __dmul_rn(a3, a3)), ffhh));
   return __dmul_rn(__dadd_rn(-B, fi_sqrt(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
+}
+
+// The update from the cell's slowness f and the spacing h.
+__device__ __forceinline__ double upd3_exact(double a1, double a2, double a3, double f, double h) {
+  return upd3_exact_core(a1, a2, a3, __dmul_rn(f, h),
+                         [&] { return __dmul_rn(__dmul_rn(__dmul_rn(f, f), h), h); });
+}
+
+// The update from the cell's fh = f h and ffhh = f f h h, each formed once in
+// the reference's order (the same bits as upd3_exact).
+__device__ __forceinline__ double upd3_exact_fh(double a1, double a2, double a3, double fh,
+                                                double ffhh) {
+  return upd3_exact_core(a1, a2, a3, fh, [&] { return ffhh; });
 }
 
 // Two-term update, reference arithmetic (Eikonal.h:14-20), given the node's
