@@ -16,6 +16,7 @@
 #include "eik3d_adj_causal.cuh"
 #include "eik3d_batch_kernels.cuh"
 #include "eik3d_common_host.h"
+#include "eik3d_single_kernels.h"
 
 namespace adt {
 
@@ -74,10 +75,15 @@ int grid1d(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, 8192));
 }
 
+// per warp: the travel-time tile with halo and the interior slowness tile
+// (FP64: two interior tiles, f h and f f h h); k_batch_fwd places the warps'
+// tiles with the same stride
 template <class T>
 size_t fwd_warp_smem(int bk) {
-  const int t = bk == 64 ? tile_elems(64) + itile_elems(64)
-                         : bk == 16 ? tile_elems(16) + itile_elems(16) : tile_elems(32) + itile_elems(32);
+  const int ni = sizeof(T) == 8 ? 2 : 1;
+  const int t = bk == 64 ? tile_elems(64) + ni * itile_elems(64)
+                         : bk == 16 ? tile_elems(16) + ni * itile_elems(16)
+                                    : tile_elems(32) + ni * itile_elems(32);
   return (size_t)t * sizeof(T);
 }
 template <class T>
@@ -108,7 +114,7 @@ struct KernelSet {
 
 template <class T>
 static KernelSet kernels_for(int bk) {
-  constexpr int MODE = sizeof(T) == 8 ? MODE_EXACT : MODE_STABLE;
+  constexpr int MODE = sizeof(T) == 8 ? MODE_EXACT_CST : MODE_STABLE;
   KernelSet k;
   if (bk == 64) {
     k.fwd = (const void*)&k_batch_fwd<T, 64, MODE>;
@@ -487,7 +493,8 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
   if ((rc = R(b, n))) return rc;
   R_(P->d_slow64, P->ncell_total * 8);
   R_(P->d_vel0, P->ncell_total * 8);
-  R_(P->d_slowT, P->f64 ? 16 : P->ncell_t_total * 4);
+  // FP32: the slowness in FP32; FP64: f h and f f h h per cell
+  R_(P->d_slowT, P->f64 ? 2 * P->ncell_total * 8 : P->ncell_t_total * 4);
   R_(P->d_sta, (size_t)sofs * 3 * 8);
   R_(P->d_tobs, P->nobs * 8);
   R_(P->d_w, P->nobs * 8);
@@ -554,7 +561,8 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].h = P->h[f];
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
       fdv[f].vel0 = P->d_vel0.as<double>() + P->cell_off[f];
-      fdv[f].f = fdv[f].f64;
+      fdv[f].f = P->d_slowT.as<double>() + 2 * P->cell_off[f];  // f h, then f f h h
+      fdv[f].f2 = fdv[f].f + P->geoms[f].ncell;
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
       fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
@@ -572,6 +580,7 @@ int batch_create(BatchPlan** out, int32_t n_fields, const int32_t* dims, const d
       fdv[f].f64 = P->d_slow64.as<double>() + P->cell_off[f];
       fdv[f].vel0 = P->d_vel0.as<double>() + P->cell_off[f];
       fdv[f].f = P->d_slowT.as<float>() + P->cell_off_t[f];  // 64-byte aligned (16-byte loads)
+      fdv[f].f2 = nullptr;
       fdv[f].bricks = P->d_levels.as<uint32_t>() + lv_off[f];
       fdv[f].lstart = P->d_lstart.as<int>() + ls_off[f];
       fdv[f].sta = P->d_sta.as<double>() + 3 * P->sta_off[f];
@@ -707,8 +716,12 @@ static int enqueue_t(BatchPlan& P, bool capturing) {
   cudaStream_t st = P.stream;
   // inside a graph capture the timing events must be external event nodes
   const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-  if (!P.f64)
-    for (int f = 0; f < P.nf; ++f)
+  for (int f = 0; f < P.nf; ++f)
+    if (P.f64)
+      k_fwd_cells<<<grid1d(P.geoms[f].ncell), 256, 0, st>>>(
+          P.d_slow64.as<double>() + P.cell_off[f], P.h[f], P.geoms[f].ncell,
+          P.d_slowT.as<double>() + 2 * P.cell_off[f]);
+    else
       k_to_t_f32<<<grid1d(P.geoms[f].ncell), 256, 0, st>>>(P.d_slow64.as<double>() + P.cell_off[f],
                                                            P.d_slowT.as<float>() + P.cell_off_t[f],
                                                            P.geoms[f].ncell);

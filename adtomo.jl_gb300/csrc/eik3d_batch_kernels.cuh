@@ -32,7 +32,9 @@ template <class T>
 struct FieldDev {
   Geom g;
   double h;
-  const T* f;               // slowness, compute precision
+  const T* f;               // FP32: slowness; FP64: f h per cell
+  const T* f2;              // FP64: f f h h per cell (f h and f f h h formed once
+                            // per evaluation in the reference's order); FP32: unused
   const double* f64;        // slowness, FP64 (gradient)
   const double* vel0;       // fixed velocity model for the near-source values, FP64
   const uint32_t* bricks;   // level-ordered bricks
@@ -473,7 +475,10 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
   const GroupCtx c = group_ctx(A, smem, META_ARRAYS_FWD);
   if (c.grp >= c.G) return;
   const int lane = c.lane;
-  T* S = reinterpret_cast<T*>(c.tiles) + c.warp * (tile_elems(BK) + itile_elems(BK));
+  // per warp: the travel-time tile, then one interior tile (f), or two with
+  // MODE_EXACT_CST (f h, f f h h); fwd_warp_smem sizes the same layout
+  constexpr int NI = MODE == MODE_EXACT_CST ? 2 : 1;
+  T* S = reinterpret_cast<T*>(c.tiles) + c.warp * (tile_elems(BK) + NI * itile_elems(BK));
   T* F = S + tile_elems(BK);
   unsigned long long cnt_upd = 0, cnt_brk = 0;
   bool first = true;
@@ -573,6 +578,8 @@ __global__ void ADT_FWD_BOUNDS k_batch_fwd(BatchArgs<T> A) {
           } else {
             load_halo_tile<T, BK>(S, u, g, p, CS, lane);
             load_interior<T, BK>(F, fd.f, g, p, CS, lane);
+            if constexpr (MODE == MODE_EXACT_CST)
+              load_interior<T, BK>(F + itile_elems(BK), fd.f2, g, p, CS, lane);
             cp_async_wait_all();
             __syncwarp();
             ch = sweep_brick_fwd<T, BK, MODE>(S, F, g, p, si, sj, sk, CS, h, fd.h, box,
