@@ -1,15 +1,15 @@
-// fp64_int.cuh -- IEEE binary64 compares, power-of-two scalings, square roots
-// and divisions evaluated on the integer and FP32 pipes, bit-identical to the
-// correctly rounded (round-to-nearest-even) FP64 operations.
+// fp64_int.cuh -- IEEE binary64 square roots and divisions evaluated on the
+// integer and FP32 pipes, bit-identical to the correctly rounded
+// (round-to-nearest-even) FP64 operations.
 //
-// GB300 executes FP64 at about 2 lanes per clock per SM: one FP64 warp
-// instruction holds its sub-partition's FP64 unit for about 64 cycles, while
-// integer and FP32 instructions issue every one or two cycles.  The
-// reference's local solves (Eikonal.h:14-20, Eikonal3D.cpp:11-28) and its
-// adjoint rows are short chains of FP64 operations.  Their compares,
-// multiplications by 2, 4 or 1/2, square roots and divisions move here.
-// Additions and general multiplications stay FP64 instructions: emulated on
-// the integer pipes they would cost about as much as the hardware one.
+// GB300 executes FP64 at about 2 lanes per clock per SM: with one warp per
+// sub-partition an FP64 addition takes about 77 cycles, and the FP64 unit's
+// square root and division sequences about 650 and 600 cycles, while integer
+// and FP32 instructions issue every one or two cycles.  The reference's local
+// solves (Eikonal.h:14-20, Eikonal3D.cpp:11-28) and its adjoint rows take
+// their square roots and divisions from here; additions, multiplications and
+// compares stay FP64 instructions, which measured faster than integer-pipe
+// versions of them in these kernels.
 //
 // Every function returns exactly the IEEE result for every input.  The
 // integer path covers finite normal operands (and zero where stated) with a
@@ -26,7 +26,8 @@
 // 53-bit result; the exact integer remainder then fixes the truncation and
 // the rounding.  Binary division and square root never land exactly halfway
 // between two doubles, so round-to-nearest needs no tie case; the division
-// keeps the even rule anyway.
+// keeps the even rule anyway.  Division by 3 takes a shorter exact route
+// (fi_div3).
 //
 // The header compiles for the host too (plain C++), where the FP32 seeds are
 // exact IEEE operations and the fallbacks are the host's IEEE operations, so
@@ -48,7 +49,6 @@ namespace adt {
 constexpr uint64_t FI_SIGN = 0x8000000000000000ull;
 constexpr uint64_t FI_FRAC = 0x000fffffffffffffull;
 constexpr uint64_t FI_HID = 0x0010000000000000ull;
-constexpr uint64_t FI_INF = 0x7ff0000000000000ull;
 
 FI_HD uint64_t fi_bits(double x) {
 #if defined(__CUDA_ARCH__)
@@ -113,62 +113,6 @@ FI_HD double fi_hw_div(double a, double b) {
 #else
   return a / b;
 #endif
-}
-
-FI_HD double fi_hw_mul(double a, double b) {
-#if defined(__CUDA_ARCH__)
-  return __dmul_rn(a, b);
-#else
-  return a * b;
-#endif
-}
-
-// ---------------------------------------------------------------- compares
-// Order key of a non-NaN double: its magnitude bits, negated for negative
-// values, so that -0 and +0 share the key 0.
-FI_HD int64_t fi_key(uint64_t b) {
-  const int64_t mag = (int64_t)(b & ~FI_SIGN);
-  return (b & FI_SIGN) ? -mag : mag;
-}
-
-FI_HD bool fi_nan(uint64_t b) { return (b & ~FI_SIGN) > FI_INF; }
-
-// a < b, IEEE semantics (false when either is NaN, -0 == +0).
-FI_HD bool fi_lt(double a, double b) {
-  const uint64_t x = fi_bits(a), y = fi_bits(b);
-  return !fi_nan(x) && !fi_nan(y) && fi_key(x) < fi_key(y);
-}
-
-// a <= b, IEEE semantics.
-FI_HD bool fi_le(double a, double b) {
-  const uint64_t x = fi_bits(a), y = fi_bits(b);
-  return !fi_nan(x) && !fi_nan(y) && fi_key(x) <= fi_key(y);
-}
-
-// a == b, IEEE semantics.
-FI_HD bool fi_eq(double a, double b) {
-  const uint64_t x = fi_bits(a), y = fi_bits(b);
-  return !fi_nan(x) && !fi_nan(y) && fi_key(x) == fi_key(y);
-}
-
-// (b < a) ? b : a -- the reference's min, selected by an integer compare.
-FI_HD double fi_min(double a, double b) { return fi_lt(b, a) ? b : a; }
-
-// |a| (clears the sign bit, as fabs does).
-FI_HD double fi_abs(double a) { return fi_double(fi_bits(a) & ~FI_SIGN); }
-
-// -------------------------------------------------------- scaling by 2^k
-// a * 2^k for k in [-2, 2], correctly rounded: the exponent field moves when
-// a and the result are normal; zero keeps its bits; else the FP64 multiply.
-template <int K>
-FI_HD double fi_scale(double a) {
-  static_assert(K >= -2 && K <= 2 && K != 0, "fi_scale: k in {-2, -1, 1, 2}");
-  const uint64_t b = fi_bits(a);
-  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
-  if (e - 1u - (K < 0 ? (uint32_t)(-K) : 0u) < 2046u - (uint32_t)(K < 0 ? -K : K))
-    return fi_double(K > 0 ? b + ((uint64_t)K << 52) : b - ((uint64_t)(-K) << 52));
-  if ((b << 1) == 0) return a;
-  return fi_hw_mul(a, K == 2 ? 4.0 : K == 1 ? 2.0 : K == -1 ? 0.5 : 0.25);
 }
 
 // -------------------------------------------------------------- square root
@@ -266,9 +210,11 @@ FI_HD double fi_div_core(uint64_t ab, uint64_t bb, float r0f) {
 
 // a / 3, correctly rounded.  For a = m 2^E (m the 53-bit significand) the
 // 53-bit quotient is floor(m 2^k / 3), k = 1 when m >= 1.5 * 2^52, else 2:
-// an exact integer division by 3 (multiply-high by 0xAAAAAAAAAAAAAAAB, then
-// a shift, exact for every 64-bit dividend), whose remainder (0, 1 or 2)
-// decides the rounding: 2/3 of a unit rounds up, 1/3 down, no ties.
+// an exact integer division by 3 (multiply-high by ceil(2^65 / 3) =
+// 0xAAAAAAAAAAAAAAAB, then a shift of one, exact for every 64-bit dividend:
+// T. Granlund, P. Montgomery, Division by Invariant Integers using
+// Multiplication, PLDI 1994), whose remainder (0, 1 or 2) decides the
+// rounding: 2/3 of a unit rounds up, 1/3 down, no ties.
 FI_HD double fi_div3(double a) {
   const uint64_t b = fi_bits(a);
   const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;

@@ -1,10 +1,9 @@
-"""The integer-pipe FP64 operations (fp64_int.cuh) built for the host, against
-IEEE binary64 arithmetic, bit for bit: square root, division (and by 3),
-compares, min, power-of-two scalings and |x|, on random operands over the whole exponent
-range, on the travel-time range the solvers see, on the hard cases of each
-operation (neighbours of exact squares and exact quotients, mantissa
-extremes) and on zeros, subnormals, infinities and NaN (which take the
-fallback).  The square root and division are also run with their FP32 seeds
+"""The integer-pipe FP64 square root and divisions (fp64_int.cuh) built for
+the host, against IEEE binary64 arithmetic, bit for bit, on random operands
+over the whole exponent range, on the travel-time range the solvers see, on
+the hard cases of each operation (neighbours of exact squares and exact
+quotients, mantissa extremes) and on zeros, subnormals, infinities and NaN
+(which take the fallback).  The square root and division are also run with their FP32 seeds
 degraded to 2^-19 relative error, far worse than the GPU's approximations,
 to show that the Newton steps and the remainder correction do not depend on
 the seed's accuracy.  CPU only; the kernels that use these operations are
@@ -125,7 +124,7 @@ def test_div3_bit_exact(lib):
                                   | np.uint64((1 << 52) - 1))])
     with np.errstate(all="ignore"):
         want = x / 3.0
-    bad = same_bits(run(lib, 11, x), want)
+    bad = same_bits(run(lib, 2, x), want)
     assert bad.size == 0, f"{bad.size} mismatches, first x={x[bad[:5]]!r}"
 
 
@@ -136,32 +135,3 @@ def test_div_bit_exact(lib, perturb):
         want = a / b
     bad = same_bits(run(lib, 1, a, b, perturb), want)
     assert bad.size == 0, f"{bad.size} mismatches, first a={a[bad[:5]]!r} b={b[bad[:5]]!r}"
-
-
-def test_compares_min_abs(lib):
-    rng = np.random.default_rng(13)
-    n = 200000
-    s = specials()
-    a = np.concatenate([random_doubles(rng, n, 0, 2047, sign=True), rng.uniform(0, 1e5, n),
-                        np.repeat(s, s.size)])
-    b = np.concatenate([random_doubles(rng, n, 0, 2047, sign=True),
-                        np.where(rng.random(n) < 0.3, a[n:2 * n], rng.uniform(0, 1e5, n)),
-                        np.tile(s, s.size)])
-    with np.errstate(invalid="ignore"):
-        for op, want in ((2, a < b), (3, a <= b), (4, a == b)):
-            got = run(lib, op, a, b)
-            assert np.array_equal(got != 0.0, want), op
-        want_min = np.where(b < a, b, a)
-    assert same_bits(run(lib, 5, a, b), want_min).size == 0
-    assert same_bits(run(lib, 10, a), np.abs(a)).size == 0
-
-
-def test_power_of_two_scaling(lib):
-    rng = np.random.default_rng(14)
-    x = np.concatenate([random_doubles(rng, 200000, 0, 2047, sign=True), specials(),
-                        from_bits(np.array([1 << 52, 2 << 52, 3 << 52, 2045 << 52, 2046 << 52,
-                                            (2046 << 52) | 5], np.uint64))])
-    with np.errstate(over="ignore", under="ignore", invalid="ignore"):
-        for op, k in ((6, 4.0), (7, 2.0), (8, 0.5), (9, 0.25)):
-            bad = same_bits(run(lib, op, x), x * k)
-            assert bad.size == 0, (op, x[bad[:5]])
