@@ -169,13 +169,15 @@ def test_2d_c1_config_forward_and_grad():
     assert np.array_equal(gf, O.eik2d_backward(gu, ur, f, ix, jx, 1.0))
 
 
-@pytest.mark.parametrize("shape,src", [((140, 150), (3, 130)), ((161, 200), (150, 7))])
+@pytest.mark.parametrize("shape,src", [((120, 121), (60, 2)), ((140, 150), (3, 130)),
+                                       ((161, 200), (150, 7))])
 def test_2d_grids_beyond_the_shared_memory_paths(shape, src):
-    """Grids of 21000 and 32200 nodes: the forward keeps its travel times and
-    change flags in shared memory up to 25600 nodes and the causal adjoint its
-    working set up to 17600, so these run the forward's shared-memory path
-    with the adjoint's global one, and both global paths.  Bit-identical to
-    the oracle, with the exact skipping of unchanged nodes in the forward."""
+    """Grids of 14520, 21000 and 32200 nodes: the forward keeps its travel
+    times and change flags in shared memory up to 25600 nodes; the adjoint
+    by levels keeps its working set there up to 17600 (the travel times too
+    up to 12200), and beyond that the causal adjoint works in global memory.
+    Bit-identical to the oracle, with the exact skipping of unchanged nodes
+    in the forward."""
     rng = np.random.default_rng(5)
     f = rng.uniform(0.4, 1.6, size=shape)
     jx, ix = src
