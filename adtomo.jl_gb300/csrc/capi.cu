@@ -1,8 +1,10 @@
 // capi.cu -- the extern "C" entry points of libadtomo_gpu.so (include/adtomo_gpu.h).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "eik2d.h"
@@ -48,21 +50,49 @@ bool finite_positive(const double* a, int64_t n) {
   return true;
 }
 
-// Host <-> device staging for the host-pointer entry points.
-struct Staging {
+// Host <-> device staging for the host-pointer entry points: per device, the
+// buffers are kept between calls (grown, never shrunk; one above 256 MiB is
+// freed when its call ends), so a repeated call allocates nothing.  A call
+// holds its device's lock while it uses them (recursive: the buffers of a
+// nested call follow the outer call's); this lock is always taken before
+// the solvers' own workspace locks.
+struct StagingPool {
+  std::recursive_mutex mu;
   std::vector<DevBuf*> bufs;
-  ~Staging() {
-    for (auto* b : bufs) delete b;
+  size_t used = 0;
+};
+StagingPool& staging_pool(int dev) {
+  static StagingPool* pools = new StagingPool[64];
+  return pools[dev & 63];
+}
+
+struct Staging {
+  StagingPool* P;
+  std::unique_lock<std::recursive_mutex> lock;
+  size_t first;
+  Staging() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    P = &staging_pool(dev);
+    lock = std::unique_lock<std::recursive_mutex>(P->mu);
+    first = P->used;
   }
-  double* alloc(size_t n, int* rc) {
-    DevBuf* b = new DevBuf();
-    bufs.push_back(b);
-    if (b->reserve(std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) {
-      *rc = set_error(ADT_ENOMEM, "cudaMalloc of %zu doubles failed", n);
+  ~Staging() {
+    for (size_t k = first; k < P->used; ++k)
+      if (P->bufs[k]->bytes > ((size_t)256 << 20)) P->bufs[k]->release();
+    P->used = first;
+  }
+  void* alloc_bytes(size_t bytes, int* rc) {
+    if (P->used == P->bufs.size()) P->bufs.push_back(new DevBuf());
+    DevBuf* b = P->bufs[P->used++];
+    if (b->reserve(std::max<size_t>(bytes, 8)) != cudaSuccess) {
+      cudaGetLastError();
+      *rc = set_error(ADT_ENOMEM, "cudaMalloc of %zu bytes failed", bytes);
       return nullptr;
     }
-    return b->as<double>();
+    return b->p;
   }
+  double* alloc(size_t n, int* rc) { return static_cast<double*>(alloc_bytes(n * sizeof(double), rc)); }
 };
 
 int check2d(int64_t m, int64_t n, int64_t srcx, int64_t srcy, double h) {
@@ -142,13 +172,13 @@ int adt_eikonal(const double* f, int64_t m, int64_t n, int64_t srcx, int64_t src
   double* df = S.alloc(N, &rc);
   double* du = df ? S.alloc(N, &rc) : nullptr;
   if (!du) return rc;
-  DevBuf src;
-  ADT_CUDA(src.reserve(2 * sizeof(int)));
+  int* dsrc = static_cast<int*>(S.alloc_bytes(2 * sizeof(int), &rc));
+  if (!dsrc) return rc;
   const int hs[2] = {(int)srcx - 1, (int)srcy - 1};
-  ADT_CUDA(cudaMemcpy(src.p, hs, sizeof hs, cudaMemcpyHostToDevice));
+  ADT_CUDA(cudaMemcpy(dsrc, hs, sizeof hs, cudaMemcpyHostToDevice));
   ADT_CUDA(cudaMemcpy(df, f, N * 8, cudaMemcpyHostToDevice));
   adt_solve_status st;
-  rc = eik2d_forward_batch(df, (int)m, (int)n, h, 1, src.as<int>(), src.as<int>() + 1, du, &st, 0);
+  rc = eik2d_forward_batch(df, (int)m, (int)n, h, 1, dsrc, dsrc + 1, du, &st, 0);
   if (rc) return rc;
   ADT_CUDA(cudaMemcpy(u, du, N * 8, cudaMemcpyDeviceToHost));
   if (status) *status = st;
@@ -173,12 +203,12 @@ int adt_eikonal_batch(const double* f, int64_t m, int64_t n, int64_t count, cons
     hs[k] = (int)srcx[k] - 1;
     hs[count + k] = (int)srcy[k] - 1;
   }
-  DevBuf src;
-  ADT_CUDA(src.reserve(hs.size() * sizeof(int)));
-  ADT_CUDA(cudaMemcpy(src.p, hs.data(), hs.size() * sizeof(int), cudaMemcpyHostToDevice));
+  int* dsrc = static_cast<int*>(S.alloc_bytes(hs.size() * sizeof(int), &rc));
+  if (!dsrc) return rc;
+  ADT_CUDA(cudaMemcpy(dsrc, hs.data(), hs.size() * sizeof(int), cudaMemcpyHostToDevice));
   ADT_CUDA(cudaMemcpy(df, f, N * 8, cudaMemcpyHostToDevice));
   std::vector<adt_solve_status> st(count);
-  rc = eik2d_forward_batch(df, (int)m, (int)n, h, (int)count, src.as<int>(), src.as<int>() + count, du,
+  rc = eik2d_forward_batch(df, (int)m, (int)n, h, (int)count, dsrc, dsrc + count, du,
                            st.data(), 0);
   if (rc) return rc;
   ADT_CUDA(cudaMemcpy(u, du, N * count * 8, cudaMemcpyDeviceToHost));
