@@ -131,12 +131,12 @@ __global__ void __launch_bounds__(512)
           double ax, by;
           if (i == 0) ax = u[c + 1];
           else if (i == m) ax = u[c - 1];
-          else ax = rmin(u[c + 1], u[c - 1]);
+          else ax = min_nn(u[c + 1], u[c - 1]);
           if (j == 0) by = u[c + w];
           else if (j == n) by = u[c - w];
-          else by = rmin(u[c - w], u[c + w]);
+          else by = min_nn(u[c - w], u[c + w]);
           const double un = upd2_exact(ax, by, k.x, k.y);
-          if (un < u[c]) {  // rmin(u[c], un)
+          if (lt_nn(un, u[c])) {  // rmin(u[c], un)
             u[c] = un;
             if (i > 0) dirty[c - 1] = 1;
             if (i < m) dirty[c + 1] = 1;

@@ -175,9 +175,15 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
     if (colok && kk >= 0 && kk < BK && k < p.nk) {
       const int kg = p.k0 + k;
       const T uo = S[own + k];
-      const T ax = rmin(S[oxp + k], S[oxm + k]);
-      const T ay = rmin(S[oyp + k], S[oym + k]);
-      const T az = rmin(S[own + k + ((kg == g.l - 1) ? -1 : 1)], S[own + k + ((kg == 0) ? 1 : -1)]);
+      // the exact modes (FP64) select by integer compares (travel times are
+      // never NaN; fp64_int.cuh), off the FP64 unit
+      auto tmin = [](T x, T y) -> T {
+        if constexpr (MODE != MODE_STABLE) return min_nn(x, y);
+        else return rmin(x, y);
+      };
+      const T ax = tmin(S[oxp + k], S[oxm + k]);
+      const T ay = tmin(S[oyp + k], S[oym + k]);
+      const T az = tmin(S[own + k + ((kg == g.l - 1) ? -1 : 1)], S[own + k + ((kg == 0) ? 1 : -1)]);
       const T fc = F[fo + k];
       T un;
       if (MODE == MODE_EXACT) {
@@ -191,9 +197,12 @@ __device__ __forceinline__ bool sweep_brick_fwd(T* S, const T* F, const Geom& g,
         else
           un = upd3_stable<T>(ax, ay, az, fc * h);
       }
-      const T v = rmin(un, uo);
+      const T v = tmin(un, uo);
       S[own + k] = v;
-      if (!(v == uo)) {
+      bool same;
+      if constexpr (MODE != MODE_STABLE) same = eq_nn(v, uo);
+      else same = v == uo;
+      if (!same) {
         changed = true;
         const T d = uo - v;
         maxdec = (d > maxdec) ? d : maxdec;

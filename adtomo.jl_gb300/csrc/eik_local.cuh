@@ -29,16 +29,16 @@ template <class FF>
 __device__ __forceinline__ double upd3_exact_core(double a1, double a2, double a3, double fh,
                                                   FF ffhh_of) {
   double t;
-  if (a1 > a2) { t = a1; a1 = a2; a2 = t; }
-  if (a1 > a3) { t = a1; a1 = a3; a3 = t; }
-  if (a2 > a3) { t = a2; a2 = a3; a3 = t; }
+  if (lt_nn(a2, a1)) { t = a1; a1 = a2; a2 = t; }
+  if (lt_nn(a3, a1)) { t = a1; a1 = a3; a3 = t; }
+  if (lt_nn(a3, a2)) { t = a2; a2 = a3; a3 = t; }
   double x = __dadd_rn(a1, fh);
-  if (x <= a2) return x;
+  if (le_nn(x, a2)) return x;
   const double ffhh = ffhh_of();
   double B = -__dadd_rn(a1, a2);
   double C = __dmul_rn(__dsub_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), ffhh), 0.5);
   x = __dmul_rn(__dadd_rn(-B, fi_sqrt(__dsub_rn(__dmul_rn(B, B), __dmul_rn(4.0, C)))), 0.5);
-  if (x <= a3) return x;
+  if (le_nn(x, a3)) return x;
   B = fi_div3(__dmul_rn(-2.0, __dadd_rn(__dadd_rn(a1, a2), a3)));
   C = fi_div3(
       __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a1, a1), __dmul_rn(a2, a2)), __dmul_rn(a3, a3)), ffhh));
@@ -65,7 +65,7 @@ __device__ __forceinline__ double upd3_exact_fh(double a1, double a2, double a3,
 // unit, shared by the SM, serialises every FP64 instruction of the four.
 __device__ __forceinline__ double upd2_exact(double a, double b, double fh, double q2) {
   const double d = fabs(__dsub_rn(a, b));
-  if (d >= fh) return __dadd_rn(rmin(a, b), fh);
+  if (le_nn(fh, d)) return __dadd_rn(min_nn(a, b), fh);
   const double ab = __dsub_rn(a, b);
   const double disc = __dsub_rn(q2, __dmul_rn(ab, ab));
   return __dmul_rn(__dadd_rn(__dadd_rn(a, b), fi_sqrt(disc)), 0.5);

@@ -7,9 +7,10 @@
 // square root and division sequences about 650 and 600 cycles, while integer
 // and FP32 instructions issue every one or two cycles.  The reference's local
 // solves (Eikonal.h:14-20, Eikonal3D.cpp:11-28) and its adjoint rows take
-// their square roots and divisions from here; additions, multiplications and
-// compares stay FP64 instructions, which measured faster than integer-pipe
-// versions of them in these kernels.
+// their square roots and divisions from here, and the exact local solves
+// their compares (for values that are never NaN); additions and
+// multiplications stay FP64 instructions, which measured faster than
+// integer-pipe versions of them in these kernels.
 //
 // Every function returns exactly the IEEE result for every input.  The
 // integer path covers finite normal operands (and zero where stated) with a
@@ -114,6 +115,29 @@ FI_HD double fi_hw_div(double a, double b) {
   return a / b;
 #endif
 }
+
+// ------------------------------------------------ compares without NaN
+// IEEE a < b, a <= b, a == b and the reference's min (b < a ? b : a) for
+// doubles that are not NaN (travel times and their candidates never are):
+// the bit patterns as two's complement keys (a negative value's magnitude
+// bits flipped) compared as integers, with -0 and +0 kept equal.  A few
+// integer instructions, where an FP64 compare is a trip through the FP64
+// unit.
+FI_HD int64_t fi_key(uint64_t b) {
+  const int64_t x = (int64_t)b;
+  return x ^ ((x >> 63) & (int64_t)0x7fffffffffffffffLL);
+}
+FI_HD bool fi_both_zero(uint64_t x, uint64_t y) { return ((x | y) << 1) == 0; }
+FI_HD bool lt_nn(double a, double b) {
+  const uint64_t x = fi_bits(a), y = fi_bits(b);
+  return fi_key(x) < fi_key(y) && !fi_both_zero(x, y);
+}
+FI_HD bool le_nn(double a, double b) { return !lt_nn(b, a); }
+FI_HD bool eq_nn(double a, double b) {
+  const uint64_t x = fi_bits(a), y = fi_bits(b);
+  return x == y || fi_both_zero(x, y);
+}
+FI_HD double min_nn(double a, double b) { return lt_nn(b, a) ? b : a; }
 
 // -------------------------------------------------------------- square root
 // Integer core for a positive normal x = m 2^E (m in [2^52, 2^54), E even)

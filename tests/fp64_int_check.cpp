@@ -1,5 +1,5 @@
 // Host driver for tests/test_fp64_int.py: runs the integer-pipe FP64 square
-// roots and divisions of fp64_int.cuh on arrays (plain C++ build of the
+// roots, divisions and compares of fp64_int.cuh on arrays (plain C++ build of the
 // header) so that they can be compared bit for bit with IEEE arithmetic.  perturb != 0
 // scales each FP32 seed by 1 +- perturb (sign from the operand bits), which
 // checks that the Newton steps and the remainder correction tolerate a seed
@@ -40,7 +40,7 @@ double div_seeded(double a, double b, double perturb) {
 }
 }  // namespace
 
-// op: 0 sqrt(a), 1 a / b, 2 a / 3
+// op: 0 sqrt(a), 1 a / b, 2 a / 3, 3 a < b, 4 a <= b, 5 a == b, 6 min(a, b)
 extern "C" int fi_check_run(int op, const double* a, const double* b, double* out, int64_t n,
                             double perturb) {
   for (int64_t i = 0; i < n; ++i) {
@@ -49,6 +49,10 @@ extern "C" int fi_check_run(int op, const double* a, const double* b, double* ou
       case 0: r = sqrt_seeded(a[i], perturb); break;
       case 1: r = div_seeded(a[i], b[i], perturb); break;
       case 2: r = fi_div3(a[i]); break;
+      case 3: r = lt_nn(a[i], b[i]) ? 1.0 : 0.0; break;
+      case 4: r = le_nn(a[i], b[i]) ? 1.0 : 0.0; break;
+      case 5: r = eq_nn(a[i], b[i]) ? 1.0 : 0.0; break;
+      case 6: r = min_nn(a[i], b[i]); break;
       default: return -1;
     }
     out[i] = r;

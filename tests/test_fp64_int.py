@@ -1,5 +1,5 @@
-"""The integer-pipe FP64 square root and divisions (fp64_int.cuh) built for
-the host, against IEEE binary64 arithmetic, bit for bit, on random operands
+"""The integer-pipe FP64 square root, divisions and compares (fp64_int.cuh)
+built for the host, against IEEE binary64 arithmetic, bit for bit, on random operands
 over the whole exponent range, on the travel-time range the solvers see, on
 the hard cases of each operation (neighbours of exact squares and exact
 quotients, mantissa extremes) and on zeros, subnormals, infinities and NaN
@@ -135,3 +135,21 @@ def test_div_bit_exact(lib, perturb):
         want = a / b
     bad = same_bits(run(lib, 1, a, b, perturb), want)
     assert bad.size == 0, f"{bad.size} mismatches, first a={a[bad[:5]]!r} b={b[bad[:5]]!r}"
+
+
+def test_compares_without_nan(lib):
+    """a < b, a <= b, a == b and min(a, b) = (b < a ? b : a) for non-NaN
+    doubles: signed values over the whole range, subnormals, infinities, both
+    zeros, equal pairs."""
+    rng = np.random.default_rng(16)
+    n = 300000
+    s = specials()
+    s = s[~np.isnan(s)]
+    a = np.concatenate([random_doubles(rng, n, 0, 2046, sign=True), rng.uniform(0, 1e5, n),
+                        np.repeat(s, s.size), np.array([0.0, -0.0, 0.0, -0.0, np.inf, -np.inf])])
+    b = np.concatenate([random_doubles(rng, n, 0, 2046, sign=True),
+                        np.where(rng.random(n) < 0.3, a[n:2 * n], rng.uniform(0, 1e5, n)),
+                        np.tile(s, s.size), np.array([-0.0, 0.0, 0.0, -0.0, np.inf, np.inf])])
+    for op, want in ((3, a < b), (4, a <= b), (5, a == b)):
+        assert np.array_equal(run(lib, op, a, b) != 0.0, want), op
+    assert same_bits(run(lib, 6, a, b), np.where(b < a, b, a)).size == 0
