@@ -69,7 +69,12 @@ int adt_abi_struct_sizes(int64_t* out, int n);
  * index arithmetic; ADT_EINVAL for another bk. */
 int adt_tile_layout(int32_t bk, int32_t* out);
 
-/* ------------------------------------------------------------------------
+/* The plain ops below take host buffers.  Per device they keep their device
+ * staging buffers and solver workspaces between calls (grown to the largest
+ * grid seen, never shrunk; a staging buffer above 256 MiB is freed when its
+ * call ends), and calls on one device run one at a time.
+ *
+ * ------------------------------------------------------------------------
  * 2D op: replaces Eikonal (Eikonal.cpp:20-46, Compute :74-127).
  * f: slowness, (n+1)*(m+1) doubles; srcx, srcy: 1-based source node (the op
  * subtracts 1, Eikonal.cpp:125); h: grid spacing.  u: travel times out.
